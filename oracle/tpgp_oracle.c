@@ -1,0 +1,446 @@
+/*
+ * CPU oracle for the Pauli-propagation branch step.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file restates, in plain C, the reference
+ * engine's CPU algorithm for one secular two-spin rotation of a sparse Pauli
+ * map (DDevol engine/src/tpgp_rev.c).  It is the parity checker for the CUDA
+ * path and the CPU baseline timed by bench.py; no product code path links or
+ * calls it.  Only tests/, __graft_entry__.smoke() and bench.py load it.
+ *
+ * Parity is pinned: tests/golden/make_golden.py runs the reference's own
+ * engine (compiled from its sources by oracle/Makefile into oracle/_ref/) on
+ * seeded inputs and stores the results under tests/golden/; the CPU test
+ * suite checks this oracle against those fixtures bit for bit.
+ *
+ * Arithmetic is IEEE binary64, round-to-nearest, compiled without fast-math
+ * and without FMA contraction (-ffp-contract=off), as the reference requires
+ * (engine/CMakeLists.txt:47).
+ *
+ * Map layout (engine/include/tpgp_rev.h:25-29): keys[k*n_words + w], two
+ * bits per site (I=0, X=1, Y=2, Z=3), site s in word s/32 at bit 2*(s%32);
+ * keys strictly ascending with the highest word most significant
+ * (engine/src/tpgp_rev.c:64-72); no stored zeros.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Status codes follow tpgp_status (engine/include/tpgp_rev.h:9-17). */
+enum { ORC_OK = 0, ORC_EINVAL, ORC_ENOMEM, ORC_ECAP, ORC_ENUMERIC, ORC_EBACKEND, ORC_EBUDGET };
+
+/* Same field order as tpgp_map / tpgp_ledger / tpgp_term (tpgp_rev.h:25-51). */
+typedef struct {
+    size_t n_spins, n_words, len, capacity;
+    uint64_t *keys;
+    double *values;
+} orc_map;
+typedef struct {
+    size_t i, j;
+    unsigned qi, qj;
+    double h;
+    size_t layer;
+} orc_term;
+typedef struct {
+    double dropped_l1, dropped_l2, dropped_l2_squared;
+    double arithmetic_l2;
+    size_t rotations, removal_events, peak_terms;
+    int arithmetic_enclosed;
+} orc_ledger;
+
+/* Directed-rounding helpers: tpgp_rev.c:25-42. */
+static double up_add(double a, double b) {
+    if (a == 0)
+        return b;
+    if (b == 0)
+        return a;
+    return nextafter(a + b, INFINITY);
+}
+static double up_mul(double a, double b) {
+    if (a == 0 || b == 0)
+        return 0;
+    return nextafter(a * b, INFINITY);
+}
+static double rounding_radius(double x) {
+    if (!isfinite(x))
+        return INFINITY;
+    double above = fabs(nextafter(x, INFINITY) - x), below = fabs(x - nextafter(x, -INFINITY));
+    return above > below ? above : below;
+}
+
+/* Multi-word key order, highest word most significant: tpgp_rev.c:64-72. */
+static int key_order(const uint64_t *a, const uint64_t *b, size_t words) {
+    for (size_t w = words; w-- > 0;) {
+        if (a[w] != b[w])
+            return a[w] < b[w] ? -1 : 1;
+    }
+    return 0;
+}
+static unsigned site_symbol(const uint64_t *key, size_t site) {
+    return (unsigned)(key[site / 32] >> (2 * (site % 32))) & 3u;
+}
+/* Exponent of i in Q*P for single-site Paulis: tpgp_rev.c:414-417. */
+static unsigned phase_of(unsigned q, unsigned p) {
+    if (!q || !p || q == p)
+        return 0;
+    /* cyclic X->Y->Z->X gives +i (exponent 1), anticyclic gives -i (3) */
+    return ((q % 3) + 1 == p) ? 1u : 3u;
+}
+static int anticommutes(unsigned q, unsigned p) { return q && p && q != p; }
+
+void orc_trig(double h, double duration, double *c, double *s) {
+    /* tpgp_rev.c:528-532: x evaluated as (2*h)*duration, host libm. */
+    double x = 2 * h * duration;
+    *c = cos(x);
+    *s = sin(x);
+}
+
+void orc_map_free(orc_map *m) {
+    if (!m)
+        return;
+    free(m->keys);
+    free(m->values);
+    memset(m, 0, sizeof(*m));
+}
+
+/* Builds a map from caller arrays (copied).  No validation beyond sizes:
+ * the caller states the invariants it wants checked. */
+int orc_map_from_arrays(orc_map *m, size_t n_spins, const uint64_t *keys, const double *values,
+                        size_t len) {
+    memset(m, 0, sizeof(*m));
+    if (!n_spins)
+        return ORC_EINVAL;
+    m->n_spins = n_spins;
+    m->n_words = (n_spins + 31) / 32;
+    size_t cap = len ? len : 1;
+    m->keys = malloc(cap * m->n_words * sizeof(uint64_t));
+    m->values = malloc(cap * sizeof(double));
+    if (!m->keys || !m->values) {
+        orc_map_free(m);
+        return ORC_ENOMEM;
+    }
+    m->capacity = cap;
+    m->len = len;
+    if (len) {
+        memcpy(m->keys, keys, len * m->n_words * sizeof(uint64_t));
+        memcpy(m->values, values, len * sizeof(double));
+    }
+    return ORC_OK;
+}
+
+/*
+ * Raw branch of `count` terms into slots 2k, 2k+1 (tpgp_rev.c:432-467; the
+ * CUDA ABI's contract is engine/include/tpgp_cuda_rev.h:26-41).  Returns 1
+ * for nonzero padding bits and 4 for nonfinite inputs or outputs, as the
+ * CUDA branch backend does (engine/src/cuda_rev.cu:88,94,112-113,254-256).
+ */
+int orc_branches(const uint64_t *keys, const double *values, size_t count, size_t words,
+                 size_t spins, size_t i, size_t j, unsigned qi, unsigned qj, double c, double s,
+                 double rc, double rs, int enclose, uint64_t *out_keys, double *out_values,
+                 double *out_radii) {
+    int padding = 0, nonfinite = 0;
+    size_t rem = spins % 32;
+    for (size_t k = 0; k < count; k++) {
+        const uint64_t *key = keys + k * words;
+        uint64_t *first = out_keys + 2 * k * words, *second = first + words;
+        if (rem && (key[words - 1] >> (2 * rem)))
+            padding = 1;
+        memcpy(first, key, words * sizeof(uint64_t));
+        memcpy(second, key, words * sizeof(uint64_t));
+        double v = values[k];
+        if (!isfinite(v))
+            nonfinite = 1;
+        unsigned pi = site_symbol(key, i), pj = site_symbol(key, j);
+        out_radii[2 * k] = out_radii[2 * k + 1] = 0;
+        if (!(anticommutes(qi, pi) ^ anticommutes(qj, pj))) {
+            out_values[2 * k] = v;
+            out_values[2 * k + 1] = 0;
+            continue;
+        }
+        unsigned phase = (phase_of(qi, pi) + phase_of(qj, pj)) & 3u;
+        second[i / 32] ^= (uint64_t)qi << (2 * (i % 32));
+        second[j / 32] ^= (uint64_t)qj << (2 * (j % 32));
+        double x = v * c, y = v * s;
+        out_values[2 * k] = x;
+        out_values[2 * k + 1] = (phase == 1 ? 1.0 : -1.0) * y;
+        if (enclose) {
+            out_radii[2 * k] = up_add(up_mul(fabs(v), rc), rounding_radius(x));
+            out_radii[2 * k + 1] = up_add(up_mul(fabs(v), rs), rounding_radius(y));
+        }
+        if (!isfinite(x) || !isfinite(y) || !isfinite(out_radii[2 * k]) ||
+            !isfinite(out_radii[2 * k + 1]))
+            nonfinite = 1;
+    }
+    return padding ? 1 : nonfinite ? 4 : 0;
+}
+
+static int size_mul(size_t a, size_t b, size_t *out) {
+    if (b && a > SIZE_MAX / b)
+        return 0;
+    *out = a * b;
+    return 1;
+}
+
+/*
+ * One non-validated rotation exp(-i theta Q) . exp(+i theta Q), theta = h *
+ * duration (tpgp_rev.c:535-771 with validated = 0, so every radius is zero
+ * and arithmetic_l2 is unchanged).  Transactional: the map and ledger change
+ * only on success.  `threads` > 1 splits the branch loop across OpenMP
+ * threads, exactly the part the reference parallelises (tpgp_rev.c:641-679).
+ */
+int orc_rotate(orc_map *map, size_t i, size_t j, unsigned qi, unsigned qj, double h,
+               double duration, double threshold, size_t max_terms, double max_drop_l2,
+               unsigned threads, orc_ledger *ledger) {
+    if (!map || !ledger || !map->n_spins || map->n_words != (map->n_spins + 31) / 32 ||
+        i >= map->n_spins || j >= map->n_spins || i == j || qi > 3 || qj > 3 || !isfinite(h) ||
+        !isfinite(duration) || !isfinite(threshold) || threshold < 0 || !isfinite(max_drop_l2) ||
+        max_drop_l2 < 0 || threads == 0)
+        return ORC_EINVAL;
+    if (!isfinite(ledger->dropped_l1) || ledger->dropped_l1 < 0 || !isfinite(ledger->dropped_l2) ||
+        ledger->dropped_l2 < 0 || !isfinite(ledger->dropped_l2_squared) ||
+        ledger->dropped_l2_squared < 0 || !isfinite(ledger->arithmetic_l2) ||
+        ledger->arithmetic_l2 < 0)
+        return ORC_EINVAL;
+    double c, s;
+    if (!isfinite(2 * h * duration))
+        return ORC_ENUMERIC;
+    orc_trig(h, duration, &c, &s);
+    if (h == 0 || duration == 0 || map->len == 0)
+        return ORC_OK;
+    const size_t words = map->n_words, n = map->len;
+    if (n > SIZE_MAX / 2)
+        return ORC_ENOMEM;
+    const size_t slots = 2 * n;
+    size_t key_bytes;
+    if (!size_mul(slots, words * sizeof(uint64_t), &key_bytes))
+        return ORC_ENOMEM;
+    uint64_t *raw_keys = malloc(key_bytes), *out_keys = malloc(key_bytes);
+    double *raw_values = malloc(slots * sizeof(double)), *out_values = malloc(slots * sizeof(double));
+    double *removed = malloc(slots * sizeof(double));
+    size_t *idx = malloc(slots * sizeof(size_t)), *tmp = malloc(slots * sizeof(size_t));
+    int status = ORC_OK;
+    if (!raw_keys || !out_keys || !raw_values || !out_values || !removed || !idx || !tmp) {
+        status = ORC_ENOMEM;
+        goto out;
+    }
+    /* branch (the only parallel part, as in the reference) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1)
+#endif
+    for (size_t k = 0; k < n; k++) {
+        const uint64_t *key = map->keys + k * words;
+        uint64_t *first = raw_keys + 2 * k * words, *second = first + words;
+        memcpy(first, key, words * sizeof(uint64_t));
+        memcpy(second, key, words * sizeof(uint64_t));
+        double v = map->values[k];
+        unsigned pi = site_symbol(key, i), pj = site_symbol(key, j);
+        if (!(anticommutes(qi, pi) ^ anticommutes(qj, pj))) {
+            raw_values[2 * k] = v;
+            raw_values[2 * k + 1] = 0;
+            continue;
+        }
+        unsigned phase = (phase_of(qi, pi) + phase_of(qj, pj)) & 3u;
+        second[i / 32] ^= (uint64_t)qi << (2 * (i % 32));
+        second[j / 32] ^= (uint64_t)qj << (2 * (j % 32));
+        raw_values[2 * k] = v * c;
+        raw_values[2 * k + 1] = (phase == 1 ? 1.0 : -1.0) * (v * s);
+    }
+    /* finite check (tpgp_rev.c:682-688) */
+    for (size_t k = 0; k < slots; k++) {
+        if (!isfinite(raw_values[k])) {
+            status = ORC_ENUMERIC;
+            goto out;
+        }
+        idx[k] = k;
+    }
+    /* Stable bottom-up merge sort of slot indices by key.  The reference uses
+     * a top-down stable merge sort (tpgp_rev.c:468-483); a stable sort's
+     * output permutation is unique, so both give the same order. */
+    {
+        size_t *a = idx, *b = tmp;
+        for (size_t width = 1; width < slots; width *= 2) {
+            for (size_t lo = 0; lo < slots; lo += 2 * width) {
+                size_t mid = lo + width < slots ? lo + width : slots;
+                size_t hi = lo + 2 * width < slots ? lo + 2 * width : slots;
+                size_t x = lo, y = mid, o = lo;
+                while (x < mid && y < hi) {
+                    if (key_order(raw_keys + a[x] * words, raw_keys + a[y] * words, words) <= 0)
+                        b[o++] = a[x++];
+                    else
+                        b[o++] = a[y++];
+                }
+                while (x < mid)
+                    b[o++] = a[x++];
+                while (y < hi)
+                    b[o++] = a[y++];
+            }
+            size_t *t = a;
+            a = b;
+            b = t;
+        }
+        if (a != idx)
+            memcpy(idx, a, slots * sizeof(size_t));
+    }
+    /* merge duplicates, drop exact zeros, threshold with ledger (tpgp_rev.c:693-729) */
+    size_t out_len = 0, discarded = 0;
+    double l1 = 0, sq = 0;
+    for (size_t k = 0; k < slots;) {
+        size_t p = idx[k++];
+        const uint64_t *key = raw_keys + p * words;
+        double v = raw_values[p];
+        while (k < slots && key_order(key, raw_keys + idx[k] * words, words) == 0)
+            v += raw_values[idx[k++]];
+        if (!isfinite(v)) {
+            status = ORC_ENUMERIC;
+            goto out;
+        }
+        if (v == 0)
+            continue;
+        int identity = 1;
+        for (size_t w = 0; w < words; w++)
+            identity &= key[w] == 0;
+        if (!identity && fabs(v) <= threshold) {
+            removed[discarded++] = fabs(v);
+            l1 = up_add(l1, fabs(v));
+            sq = up_add(sq, up_mul(v, v));
+            continue;
+        }
+        memcpy(out_keys + out_len * words, key, words * sizeof(uint64_t));
+        out_values[out_len++] = v;
+    }
+    /* cap, ledger, budget, commit (tpgp_rev.c:730-757); the removed-L2 bound
+     * is the non-MPFR upper_l2 (tpgp_rev.c:58-61) */
+    if (max_terms && out_len > max_terms) {
+        status = ORC_ECAP;
+        goto out;
+    }
+    {
+        double sum = 0;
+        for (size_t k = 0; k < discarded; k++)
+            sum = up_add(sum, up_mul(removed[k], removed[k]));
+        double l2 = sum == 0 ? 0 : nextafter(sqrt(sum), INFINITY);
+        orc_ledger next = *ledger;
+        next.dropped_l1 = up_add(next.dropped_l1, l1);
+        next.dropped_l2 = up_add(next.dropped_l2, l2);
+        next.dropped_l2_squared = up_add(next.dropped_l2_squared, sq);
+        next.arithmetic_l2 = up_add(next.arithmetic_l2, 0);
+        next.rotations++;
+        if (discarded)
+            next.removal_events++;
+        if (out_len > next.peak_terms)
+            next.peak_terms = out_len;
+        next.arithmetic_enclosed = 0;
+        if (!isfinite(next.dropped_l2) || !isfinite(next.arithmetic_l2)) {
+            status = ORC_ENUMERIC;
+            goto out;
+        }
+        if (max_drop_l2 && next.dropped_l2 > max_drop_l2) {
+            status = ORC_EBUDGET;
+            goto out;
+        }
+        free(map->keys);
+        free(map->values);
+        map->keys = out_keys;
+        map->values = out_values;
+        map->len = out_len;
+        map->capacity = slots;
+        out_keys = NULL;
+        out_values = NULL;
+        *ledger = next;
+    }
+out:
+    free(raw_keys);
+    free(out_keys);
+    free(raw_values);
+    free(out_values);
+    free(removed);
+    free(idx);
+    free(tmp);
+    return status;
+}
+
+static int map_copy(orc_map *dst, const orc_map *src) {
+    return orc_map_from_arrays(dst, src->n_spins, src->keys, src->values, src->len);
+}
+
+/* Symmetric Strang product (tpgp_rev.c:776-809): terms forward at dt/2,
+ * then backward at dt/2; transactional over the whole step. */
+int orc_strang_step(orc_map *map, const orc_term *terms, size_t count, double dt, double threshold,
+                    size_t max_terms, double max_drop_l2, unsigned threads, orc_ledger *ledger) {
+    if (!map || (!terms && count) || !ledger || !isfinite(dt))
+        return ORC_EINVAL;
+    double half = dt * 0.5;
+    if (half * 2 != dt)
+        return ORC_ENUMERIC;
+    orc_map work;
+    int status = map_copy(&work, map);
+    if (status)
+        return status;
+    orc_ledger next = *ledger;
+    for (size_t k = 0; k < 2 * count && !status; k++) {
+        const orc_term *t = k < count ? terms + k : terms + (2 * count - 1 - k);
+        status = orc_rotate(&work, t->i, t->j, t->qi, t->qj, t->h, half, threshold, max_terms,
+                            max_drop_l2, threads, &next);
+    }
+    if (status) {
+        orc_map_free(&work);
+        return status;
+    }
+    orc_map_free(map);
+    *map = work;
+    *ledger = next;
+    return ORC_OK;
+}
+
+/* Compensated long-double sum of coefficients whose key has Pauli weight 1
+ * with symbol p (tpgp_rev.c:311-338). */
+double orc_single_sum(const orc_map *m, unsigned p) {
+    if (p < 1 || p > 3)
+        return NAN;
+    long double sum = 0, correction = 0;
+    for (size_t k = 0; k < m->len; k++) {
+        unsigned weight = 0, symbol = 0;
+        for (size_t w = 0; w < m->n_words; w++) {
+            for (uint64_t q = m->keys[k * m->n_words + w]; q; q >>= 2) {
+                if (q & 3u) {
+                    weight++;
+                    symbol = (unsigned)(q & 3u);
+                }
+            }
+        }
+        if (weight != 1 || symbol != p)
+            continue;
+        long double value = m->values[k], next = sum + value;
+        if (fabsl(sum) >= fabsl(value))
+            correction += (sum - next) + value;
+        else
+            correction += (value - next) + sum;
+        sum = next;
+    }
+    return (double)(sum + correction);
+}
+
+/* Same reduction over caller arrays (used to check the device readout). */
+double orc_single_sum_arrays(const uint64_t *keys, const double *values, size_t len,
+                             size_t n_spins, unsigned p) {
+    orc_map view = {n_spins, (n_spins + 31) / 32, len, len, (uint64_t *)keys, (double *)values};
+    return orc_single_sum(&view, p);
+}
+
+int orc_has_openmp(void) {
+#ifdef _OPENMP
+    return 1;
+#else
+    return 0;
+#endif
+}
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
