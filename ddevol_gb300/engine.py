@@ -1,0 +1,218 @@
+"""Python mirror of the reference engine's operator interface, on the GB300 library.
+
+The names follow DDevol's C API (engine/include/tpgp_rev.h and
+engine/include/tpgp_cuda_rev.h) so that tests and drivers read like the
+reference's own:
+
+* :class:`CudaBranchContext` -- ``tpgp_cuda_create`` / ``tpgp_cuda_branches``
+  (the raw branch backend the reference engine calls per rotation);
+* :class:`Engine` / :class:`DeviceMap` -- a device-resident ``tpgp_map`` with
+  ``rotate`` (``tpgp_rotate``), ``strang_step`` (``tpgp_strang_step``),
+  ``evolve`` (the CLI time loop) and ``single_sum`` (``tpgp_map_single_sum``).
+
+Statuses are returned as the reference's integers (0 = ok, 1 = EINVAL, ...);
+``STATUS_NAMES`` maps them to names.  Every call runs on the GPU; nothing
+here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native
+from .native import CUDA_STATUS_NAMES, STATUS_NAMES, GbLedger, GbOptions, GbTerm
+
+__all__ = ["CudaBranchContext", "Engine", "DeviceMap", "options", "terms_array",
+           "STATUS_NAMES", "CUDA_STATUS_NAMES", "GbLedger"]
+
+
+def _u64p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+def _f64p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def options(threshold=0.0, max_terms=0, max_drop_l2=0.0, exact_ledger=True, use_graphs=True):
+    return GbOptions(float(threshold), int(max_terms), float(max_drop_l2), int(bool(exact_ledger)),
+                     int(bool(use_graphs)))
+
+
+def terms_array(terms):
+    terms = list(terms)
+    arr = (GbTerm * max(1, len(terms)))()
+    for k, (i, j, qi, qj, h) in enumerate(terms):
+        arr[k] = GbTerm(i, j, qi, qj, h, k)
+    return arr, len(terms)
+
+
+class CudaBranchContext:
+    """Reference-compatible branch backend context (tpgp_cuda_rev.h)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = native.load()
+        err = C.create_string_buffer(512)
+        self.ptr = self.lib.tpgp_cuda_create(device, err, len(err))
+        if not self.ptr:
+            raise RuntimeError(f"tpgp_cuda_create failed: {err.value.decode()}")
+
+    @property
+    def name(self) -> str:
+        return self.lib.tpgp_cuda_device_name(self.ptr).decode()
+
+    def branches(self, keys, values, n_spins, i, j, qi, qj, c, s, rc=0.0, rs=0.0, enclose=0,
+                 words=None):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        words = (n_spins + 31) // 32 if words is None else words
+        count = len(values)
+        ok = np.zeros(max(1, 2 * count * words), np.uint64)
+        ov = np.zeros(max(1, 2 * count), np.float64)
+        orad = np.zeros(max(1, 2 * count), np.float64)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_cuda_branches(self.ptr, _u64p(keys), _f64p(values), count, words,
+                                         n_spins, i, j, qi, qj, c, s, rc, rs, enclose, _u64p(ok),
+                                         _f64p(ov), _f64p(orad), err, len(err))
+        return st, ok[:2 * count * words], ov[:2 * count], orad[:2 * count], err.value.decode()
+
+    def close(self):
+        if self.ptr:
+            self.lib.tpgp_cuda_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    """One GB300 device and stream (tpgp_gb_create)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = native.load()
+        err = C.create_string_buffer(512)
+        self.ptr = self.lib.tpgp_gb_create(device, err, len(err))
+        if not self.ptr:
+            raise RuntimeError(f"tpgp_gb_create failed: {err.value.decode()}")
+
+    @property
+    def name(self) -> str:
+        return self.lib.tpgp_gb_device_name(self.ptr).decode()
+
+    def map(self, n_spins: int, keys=None, values=None) -> "DeviceMap":
+        m = DeviceMap(self, n_spins)
+        if keys is not None:
+            st, msg = m.upload(keys, values)
+            if st:
+                m.close()
+                raise ValueError(f"upload failed ({STATUS_NAMES[st]}): {msg}")
+        return m
+
+    def close(self):
+        if self.ptr:
+            self.lib.tpgp_gb_destroy(self.ptr)
+            self.ptr = None
+
+
+class DeviceMap:
+    """A tpgp_map kept in HBM between rotations (tpgp_gb_map)."""
+
+    def __init__(self, engine: Engine, n_spins: int):
+        self.engine = engine
+        self.lib = engine.lib
+        self.n_spins = n_spins
+        self.n_words = (n_spins + 31) // 32
+        ptr = C.c_void_p()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_map_create(engine.ptr, n_spins, C.byref(ptr), err, len(err))
+        if st:
+            raise RuntimeError(f"tpgp_gb_map_create failed: {err.value.decode()}")
+        self.ptr = ptr
+        self._terms_cache = (None, None, 0)
+
+    def __len__(self):
+        return self.lib.tpgp_gb_map_len(self.ptr)
+
+    def upload(self, keys, values):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_map_upload(self.ptr, _u64p(keys), _f64p(values), len(values), err,
+                                         len(err))
+        return st, err.value.decode()
+
+    def download(self):
+        n = len(self)
+        keys = np.zeros(max(1, n * self.n_words), np.uint64)
+        values = np.zeros(max(1, n), np.float64)
+        got = C.c_size_t()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_map_download(self.ptr, _u64p(keys), _f64p(values), n, C.byref(got),
+                                           err, len(err))
+        if st:
+            raise RuntimeError(f"download failed: {err.value.decode()}")
+        return keys[:got.value * self.n_words], values[:got.value]
+
+    def rotate(self, i, j, qi, qj, theta, opts=None, ledger=None):
+        opts = opts if opts is not None else options()
+        ledger = ledger if ledger is not None else GbLedger()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_rotate(self.ptr, i, j, qi, qj, theta, C.byref(opts),
+                                     C.byref(ledger), err, len(err))
+        return st, ledger, err.value.decode()
+
+    def _terms(self, terms):
+        # the ctypes array is rebuilt only when a different term list is passed
+        if self._terms_cache[0] is not terms:
+            arr, count = terms_array(terms)
+            self._terms_cache = (terms, arr, count)
+        return self._terms_cache[1], self._terms_cache[2]
+
+    def strang_step(self, terms, dt, opts=None, ledger=None):
+        opts = opts if opts is not None else options()
+        ledger = ledger if ledger is not None else GbLedger()
+        arr, count = self._terms(terms)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_strang_step(self.ptr, arr, count, dt, C.byref(opts),
+                                          C.byref(ledger), err, len(err))
+        return st, ledger, err.value.decode()
+
+    def evolve(self, terms, dt, steps, opts=None, ledger=None, record_fid=True):
+        opts = opts if opts is not None else options()
+        ledger = ledger if ledger is not None else GbLedger()
+        arr, count = self._terms(terms)
+        fids = np.zeros(max(1, steps), np.float64)
+        done = C.c_size_t()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_evolve(self.ptr, arr, count, dt, steps, C.byref(opts),
+                                     C.byref(ledger), _f64p(fids) if record_fid else None,
+                                     C.byref(done), err, len(err))
+        return st, fids[:done.value], ledger, err.value.decode()
+
+    def single_sum(self, pauli=1):
+        out = C.c_double()
+        st = self.lib.tpgp_gb_single_sum(self.ptr, pauli, C.byref(out))
+        if st:
+            raise RuntimeError(f"single_sum failed: {STATUS_NAMES[st]}")
+        return out.value
+
+    def last_elapsed_ms(self):
+        return self.lib.tpgp_gb_last_elapsed_ms(self.ptr)
+
+    def last_launches(self):
+        return self.lib.tpgp_gb_last_launches(self.ptr)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.tpgp_gb_map_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

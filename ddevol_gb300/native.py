@@ -1,0 +1,114 @@
+"""ctypes bindings of ``libtpgp_gb300.so`` (include/tpgp_cuda_rev.h, include/tpgp_gb300.h).
+
+The library is the product: every call here goes straight to the sm_103a
+kernels.  There is no CPU fallback -- if the library cannot be loaded or no
+GB300 is visible, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+STATUS_NAMES = ["ok", "einval", "enomem", "ecap", "enumeric", "ebackend", "ebudget"]
+CUDA_STATUS_NAMES = ["ok", "einval", "enomem", "edevice", "enumeric"]
+
+_lock = threading.Lock()
+_lib = None
+
+
+class GbTerm(C.Structure):
+    """tpgp_gb_term: layout of tpgp_term (engine/include/tpgp_rev.h:30-35)."""
+
+    _fields_ = [("i", C.c_size_t), ("j", C.c_size_t), ("qi", C.c_uint), ("qj", C.c_uint),
+                ("h", C.c_double), ("layer", C.c_size_t)]
+
+
+class GbLedger(C.Structure):
+    """tpgp_gb_ledger: layout of tpgp_ledger (engine/include/tpgp_rev.h:46-51)."""
+
+    _fields_ = [("dropped_l1", C.c_double), ("dropped_l2", C.c_double),
+                ("dropped_l2_squared", C.c_double), ("arithmetic_l2", C.c_double),
+                ("rotations", C.c_size_t), ("removal_events", C.c_size_t),
+                ("peak_terms", C.c_size_t), ("arithmetic_enclosed", C.c_int)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GbOptions(C.Structure):
+    _fields_ = [("threshold", C.c_double), ("max_terms", C.c_size_t),
+                ("max_drop_l2", C.c_double), ("exact_ledger", C.c_int), ("use_graphs", C.c_int)]
+
+
+def _bind(lib):
+    P = C.POINTER
+    u64p, f64p, charp = P(C.c_uint64), P(C.c_double), C.c_char_p
+    sz = C.c_size_t
+    # reference-compatible branch ABI
+    lib.tpgp_cuda_compiled.restype = C.c_int
+    lib.tpgp_cuda_create.restype = C.c_void_p
+    lib.tpgp_cuda_create.argtypes = [C.c_int, charp, sz]
+    lib.tpgp_cuda_destroy.argtypes = [C.c_void_p]
+    lib.tpgp_cuda_device_name.restype = C.c_char_p
+    lib.tpgp_cuda_device_name.argtypes = [C.c_void_p]
+    lib.tpgp_cuda_branches.restype = C.c_int
+    lib.tpgp_cuda_branches.argtypes = [
+        C.c_void_p, u64p, f64p, sz, sz, sz, sz, sz, C.c_uint, C.c_uint, C.c_double, C.c_double,
+        C.c_double, C.c_double, C.c_int, u64p, f64p, f64p, charp, sz]
+    # device-resident ABI
+    lib.tpgp_gb_compiled.restype = C.c_int
+    lib.tpgp_gb_default_options.restype = GbOptions
+    lib.tpgp_gb_create.restype = C.c_void_p
+    lib.tpgp_gb_create.argtypes = [C.c_int, charp, sz]
+    lib.tpgp_gb_destroy.argtypes = [C.c_void_p]
+    lib.tpgp_gb_device_name.restype = C.c_char_p
+    lib.tpgp_gb_device_name.argtypes = [C.c_void_p]
+    lib.tpgp_gb_map_create.restype = C.c_int
+    lib.tpgp_gb_map_create.argtypes = [C.c_void_p, sz, P(C.c_void_p), charp, sz]
+    lib.tpgp_gb_map_destroy.argtypes = [C.c_void_p]
+    lib.tpgp_gb_map_len.restype = sz
+    lib.tpgp_gb_map_len.argtypes = [C.c_void_p]
+    lib.tpgp_gb_map_spins.restype = sz
+    lib.tpgp_gb_map_spins.argtypes = [C.c_void_p]
+    lib.tpgp_gb_map_upload.restype = C.c_int
+    lib.tpgp_gb_map_upload.argtypes = [C.c_void_p, u64p, f64p, sz, charp, sz]
+    lib.tpgp_gb_map_download.restype = C.c_int
+    lib.tpgp_gb_map_download.argtypes = [C.c_void_p, u64p, f64p, sz, P(sz), charp, sz]
+    lib.tpgp_gb_rotate.restype = C.c_int
+    lib.tpgp_gb_rotate.argtypes = [C.c_void_p, sz, sz, C.c_uint, C.c_uint, C.c_double,
+                                   P(GbOptions), P(GbLedger), charp, sz]
+    lib.tpgp_gb_strang_step.restype = C.c_int
+    lib.tpgp_gb_strang_step.argtypes = [C.c_void_p, P(GbTerm), sz, C.c_double, P(GbOptions),
+                                        P(GbLedger), charp, sz]
+    lib.tpgp_gb_evolve.restype = C.c_int
+    lib.tpgp_gb_evolve.argtypes = [C.c_void_p, P(GbTerm), sz, C.c_double, sz, P(GbOptions),
+                                   P(GbLedger), f64p, P(sz), charp, sz]
+    lib.tpgp_gb_single_sum.restype = C.c_int
+    lib.tpgp_gb_single_sum.argtypes = [C.c_void_p, C.c_uint, f64p]
+    lib.tpgp_gb_last_elapsed_ms.restype = C.c_double
+    lib.tpgp_gb_last_elapsed_ms.argtypes = [C.c_void_p]
+    lib.tpgp_gb_last_launches.restype = sz
+    lib.tpgp_gb_last_launches.argtypes = [C.c_void_p]
+    return lib
+
+
+def load(build_if_needed: bool = True):
+    """Loads (building first if needed) the native library; raises on failure."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_needed:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"native library missing: {path} (run ddevol_gb300.build)")
+        _lib = _bind(C.CDLL(path))
+        return _lib
+
+
+def library_path() -> str:
+    return _build.LIB

@@ -1,0 +1,146 @@
+/* Device-resident Pauli propagation on one GB300 (sm_103a).
+ *
+ * The reference engine keeps its operator as a host tpgp_map and, with the
+ * CUDA backend, ships every rotation's input to the GPU and its 2n raw
+ * children back for a host sort (DDevol engine/src/tpgp_rev.c:622-640,
+ * engine/src/cuda_rev.cu:229-264).  This interface keeps the map on the
+ * device for the whole rotation: branch, sort by key, merge of duplicates,
+ * threshold truncation and ledger all run as sm_103a kernels, and the map
+ * crosses PCIe/C2C only on upload and download.  The host map format
+ * (keys[k*n_words + w], two bits per site, strictly ascending keys, no zeros)
+ * is the reference's tpgp_map, so maps move to and from the reference
+ * engine, its checkpoint code and its readout unchanged.
+ *
+ * Each entry point cites the reference interface it stands in for.  Status
+ * codes are tpgp_status's (engine/include/tpgp_rev.h:9-17); every mutation
+ * is transactional: on failure the map and the ledger are unchanged.
+ */
+#ifndef TPGP_GB300_H
+#define TPGP_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same values as tpgp_status (engine/include/tpgp_rev.h:9-17). */
+typedef enum {
+    TPGP_GB_OK = 0,
+    TPGP_GB_EINVAL,
+    TPGP_GB_ENOMEM,
+    TPGP_GB_ECAP,
+    TPGP_GB_ENUMERIC,
+    TPGP_GB_EBACKEND,
+    TPGP_GB_EBUDGET
+} tpgp_gb_status;
+
+/* Same layout as tpgp_term (engine/include/tpgp_rev.h:30-35). */
+typedef struct {
+    size_t i, j;
+    unsigned qi, qj;
+    double h;
+    size_t layer;
+} tpgp_gb_term;
+
+/* Same layout as tpgp_ledger (engine/include/tpgp_rev.h:46-51). */
+typedef struct {
+    double dropped_l1, dropped_l2, dropped_l2_squared;
+    double arithmetic_l2;
+    size_t rotations, removal_events, peak_terms;
+    int arithmetic_enclosed;
+} tpgp_gb_ledger;
+
+/* Rotation options; threshold, max_terms and max_drop_l2 mean what they mean
+ * in tpgp_options (engine/include/tpgp_rev.h:36-45).
+ *   exact_ledger = 1: the removed-weight sums are accumulated in the
+ *     reference's sequential key order, so the ledger is bitwise equal to the
+ *     CPU engine's; one GPU thread walks the removed terms of each rotation.
+ *   exact_ledger = 0: the sums are deterministic fixed-shape trees of
+ *     upward-rounded additions.  Every partial sum is rounded up, so each
+ *     ledger entry is still a rigorous upper bound on the removed weight; it
+ *     differs from the sequential sum by at most 3 n_removed 2^-53 relative.
+ *   use_graphs = 1: each Strang step's kernel sequence is captured once as a
+ *     CUDA graph and replayed. */
+typedef struct {
+    double threshold;
+    size_t max_terms;
+    double max_drop_l2;
+    int exact_ledger;
+    int use_graphs;
+} tpgp_gb_options;
+
+typedef struct tpgp_gb_context tpgp_gb_context;
+typedef struct tpgp_gb_map tpgp_gb_map;
+
+/* Library and device.  compiled() is 1 for this build.  create() binds one
+ * device (index as CUDA_VISIBLE_DEVICES numbers it) and a stream; NULL with
+ * a message when the device is missing.  Replaces the context part of
+ * engine/include/tpgp_cuda_rev.h:20-23 for the device-resident path. */
+int tpgp_gb_compiled(void);
+tpgp_gb_options tpgp_gb_default_options(void);
+tpgp_gb_context *tpgp_gb_create(int device_index, char *error, size_t error_capacity);
+void tpgp_gb_destroy(tpgp_gb_context *context);
+const char *tpgp_gb_device_name(const tpgp_gb_context *context);
+
+/* Device maps.  Stand-ins for tpgp_map_init / tpgp_map_free / the map's
+ * storage (engine/include/tpgp_rev.h:25-29, 60-61).  n_spins >= 2 and at
+ * most 128 (keys of up to four 64-bit words). */
+tpgp_gb_status tpgp_gb_map_create(tpgp_gb_context *context, size_t n_spins, tpgp_gb_map **map,
+                                  char *error, size_t error_capacity);
+void tpgp_gb_map_destroy(tpgp_gb_map *map);
+size_t tpgp_gb_map_len(const tpgp_gb_map *map);
+size_t tpgp_gb_map_spins(const tpgp_gb_map *map);
+
+/* Replaces the map's contents with `len` host terms.  The terms must satisfy
+ * the tpgp_map invariants the reference's tpgp_map_add enforces
+ * (engine/src/tpgp_rev.c:73-83, 206-210): keys strictly ascending, zero
+ * padding bits, finite nonzero values.  EINVAL otherwise (map unchanged). */
+tpgp_gb_status tpgp_gb_map_upload(tpgp_gb_map *map, const uint64_t *keys, const double *values,
+                                  size_t len, char *error, size_t error_capacity);
+
+/* Copies the map to host arrays of room for `capacity` terms; *len receives
+ * the term count.  EINVAL (nothing copied) if capacity < len. */
+tpgp_gb_status tpgp_gb_map_download(const tpgp_gb_map *map, uint64_t *keys, double *values,
+                                    size_t capacity, size_t *len, char *error,
+                                    size_t error_capacity);
+
+/* One rotation exp(-i theta Q) A exp(+i theta Q), Q = sigma^qi_i sigma^qj_j.
+ * Same contract as tpgp_rotate (engine/include/tpgp_rev.h:84-85,
+ * engine/src/tpgp_rev.c:772-775) with the non-validated backend: keys,
+ * values, cap, budget and statuses are the reference's. */
+tpgp_gb_status tpgp_gb_rotate(tpgp_gb_map *map, size_t i, size_t j, unsigned qi, unsigned qj,
+                              double theta, const tpgp_gb_options *options,
+                              tpgp_gb_ledger *ledger, char *error, size_t error_capacity);
+
+/* Symmetric Strang step: terms forward at dt/2, then backward at dt/2.
+ * Same contract as tpgp_strang_step (engine/include/tpgp_rev.h:86-87,
+ * engine/src/tpgp_rev.c:776-809). */
+tpgp_gb_status tpgp_gb_strang_step(tpgp_gb_map *map, const tpgp_gb_term *terms, size_t count,
+                                   double dt, const tpgp_gb_options *options,
+                                   tpgp_gb_ledger *ledger, char *error, size_t error_capacity);
+
+/* `steps` Strang steps in a row, the reference CLI's time loop
+ * (engine/src/cli_rev.c:575-670) without I/O: after each accepted step k
+ * (0-based) fid_sums[k] receives tpgp_gb_single_sum(map, 1) when fid_sums
+ * is not NULL.  *steps_done receives the number of accepted steps; on a
+ * failure the map and ledger hold the last accepted step. */
+tpgp_gb_status tpgp_gb_evolve(tpgp_gb_map *map, const tpgp_gb_term *terms, size_t count,
+                              double dt, size_t steps, const tpgp_gb_options *options,
+                              tpgp_gb_ledger *ledger, double *fid_sums, size_t *steps_done,
+                              char *error, size_t error_capacity);
+
+/* Compensated sum of the coefficients whose key has Pauli weight one with
+ * symbol `pauli` (1..3), bitwise equal to tpgp_map_single_sum
+ * (engine/include/tpgp_rev.h:73, engine/src/tpgp_rev.c:311-338). */
+tpgp_gb_status tpgp_gb_single_sum(const tpgp_gb_map *map, unsigned pauli, double *sum);
+
+/* Device time of the last rotation kernels, for measurement: the summed
+ * duration (ms) of the most recent tpgp_gb_strang_step / tpgp_gb_evolve
+ * call's timed region, and the number of kernel launches it issued. */
+double tpgp_gb_last_elapsed_ms(const tpgp_gb_map *map);
+size_t tpgp_gb_last_launches(const tpgp_gb_map *map);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

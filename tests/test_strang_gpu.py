@@ -1,0 +1,143 @@
+"""Strang steps and trajectories on the device against the reference and the oracle.
+
+* every golden trajectory from the reference engine (ring16 J1-J2, the
+  reference's own N=6 CUDA-trajectory case, 64-site all-pairs ring, 4x4x4
+  cubic, 96-site chain): final keys, values and ledger bitwise, the per-step
+  FID sum (tpgp_map_single_sum) bitwise, the per-step term count;
+* graph replay and plain launches give identical results;
+* the fast (tree) ledger keeps keys/values bitwise and stays within its bound;
+* transactional failures: a cap or budget hit mid-step, an invalid term after
+  valid ones, leave map and ledger untouched.
+"""
+import numpy as np
+import pytest
+
+from ddevol_gb300 import hamiltonians as H
+from ddevol_gb300.engine import GbLedger, options
+from gpu_helpers import bits, ledger_vec
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["ring16", "n6_thr0", "n6_thr1e-5", "ring64_allpairs", "cubic4", "chain96"]
+
+
+def load_traj(g, name):
+    p = name + "__"
+    terms = [(int(a), int(b), int(c), int(d), float(h))
+             for (a, b, c, d), h in zip(g[p + "terms"], g[p + "h"])]
+    return p, terms
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+@pytest.mark.parametrize("name", NAMES)
+def test_golden_trajectories(engine, golden_trajectories, name, use_graphs):
+    g = golden_trajectories
+    p, terms = load_traj(g, name)
+    m = engine.map(int(g[p + "n"]), g[p + "in_keys"], g[p + "in_values"])
+    st, fids, led, msg = m.evolve(terms, float(g[p + "dt"]), int(g[p + "steps"]),
+                                  options(float(g[p + "threshold"]), use_graphs=use_graphs))
+    assert st == 0, msg
+    k, v = m.download()
+    m.close()
+    assert np.array_equal(k, g[p + "out_keys"])
+    assert np.array_equal(bits(v), bits(g[p + "out_values"]))
+    assert np.array_equal(bits(ledger_vec(led)), bits(g[p + "ledger"]))
+    assert np.array_equal(bits(fids), bits(g[p + "fid_sum"]))
+
+
+@pytest.mark.parametrize("name", ["ring16", "cubic4", "ring64_allpairs"])
+def test_bound_ledger_trajectory(engine, golden_trajectories, name):
+    g = golden_trajectories
+    p, terms = load_traj(g, name)
+    m = engine.map(int(g[p + "n"]), g[p + "in_keys"], g[p + "in_values"])
+    st, fids, led, msg = m.evolve(terms, float(g[p + "dt"]), int(g[p + "steps"]),
+                                  options(float(g[p + "threshold"]), exact_ledger=False))
+    assert st == 0, msg
+    k, v = m.download()
+    m.close()
+    assert np.array_equal(k, g[p + "out_keys"])
+    assert np.array_equal(bits(v), bits(g[p + "out_values"]))
+    assert np.array_equal(bits(fids), bits(g[p + "fid_sum"]))
+    got, want = ledger_vec(led), g[p + "ledger"]
+    # each rotation's tree sum and the sequential sum both bound the exact sum
+    # from above within 3 k 2^-53 (k <= 2n upward additions); 1e-11 covers
+    # thousands of rotations of these sizes
+    for f in range(3):
+        assert abs(got[f] - want[f]) <= 1e-11 * want[f]
+    assert np.array_equal(got[3:], want[3:])
+
+
+def test_strang_step_matches_evolve(engine, golden_trajectories):
+    g = golden_trajectories
+    p, terms = load_traj(g, "ring16")
+    m = engine.map(16, g[p + "in_keys"], g[p + "in_values"])
+    led = GbLedger()
+    opts = options(float(g[p + "threshold"]))
+    for _ in range(int(g[p + "steps"])):
+        st, led, msg = m.strang_step(terms, float(g[p + "dt"]), opts, led)
+        assert st == 0, msg
+    k, v = m.download()
+    assert np.array_equal(k, g[p + "out_keys"])
+    assert np.array_equal(bits(v), bits(g[p + "out_values"]))
+    assert np.array_equal(bits(ledger_vec(led)), bits(g[p + "ledger"]))
+    assert m.single_sum(1) == float(g[p + "fid_sum"][-1])
+    m.close()
+
+
+def test_longer_ring16_vs_oracle(engine, oracle):
+    """60 steps of the benchmark ring (map ~45k terms): multi-tile every rotation."""
+    terms = H.ring_j1j2(16)
+    k0, v0 = H.single_site_operator(16)
+    fids_o = []
+    ost, ok, ov, oled = oracle.strang_step(k0, v0, 16, terms, 0.01, threshold=1e-6, steps=60,
+                                           threads=8, on_step=lambda s, f, n: fids_o.append(f))
+    m = engine.map(16, k0, v0)
+    st, fids, led, msg = m.evolve(terms, 0.01, 60, options(1e-6))
+    assert st == ost == 0, msg
+    k, v = m.download()
+    m.close()
+    assert len(v) > 20000
+    assert np.array_equal(k, ok) and np.array_equal(bits(v), bits(ov))
+    assert np.array_equal(bits(fids), bits(np.array(fids_o)))
+    assert led.dropped_l2 == oled.dropped_l2 and led.dropped_l1 == oled.dropped_l1
+
+
+def test_transactional_cap_and_budget(engine, golden_trajectories):
+    g = golden_trajectories
+    p, terms = load_traj(g, "ring16")
+    m = engine.map(16, g[p + "in_keys"], g[p + "in_values"])
+    k0, v0 = m.download()
+    led0 = GbLedger()
+    led0.dropped_l1 = 0.25
+    st, led, _ = m.strang_step(terms, 0.01, options(1e-6, max_terms=len(v0) + 5), led0)
+    assert st == 3  # ECAP part-way through the step
+    k, v = m.download()
+    assert np.array_equal(k, k0) and np.array_equal(bits(v), bits(v0))
+    assert led.dropped_l1 == 0.25 and led.rotations == 0
+    st, led, _ = m.strang_step(terms, 0.01, options(1e-6, max_drop_l2=1e-12), led0)
+    assert st == 6  # EBUDGET
+    k, v = m.download()
+    assert np.array_equal(k, k0) and np.array_equal(bits(v), bits(v0))
+    # an invalid term after valid ones: the valid prefix runs, the step fails
+    bad = list(terms[:5]) + [(3, 3, 1, 1, 0.1)]
+    st, led, _ = m.strang_step(bad, 0.01, options(1e-6), GbLedger())
+    assert st == 1
+    k, v = m.download()
+    assert np.array_equal(k, k0) and np.array_equal(bits(v), bits(v0))
+    st, led, _ = m.strang_step(terms, 3 * 2.0 ** -1074, options(), GbLedger())
+    assert st == 4  # dt/2 inexact
+    m.close()
+
+
+def test_growth_across_arena_resize(engine, oracle):
+    """Start from a tiny arena and grow through several reallocations in one call."""
+    terms = H.ring_j1j2(8)
+    k0, v0 = H.global_x_operator(8)
+    ost, ok, ov, _ = oracle.strang_step(k0, v0, 8, terms, 0.05, threshold=0.0, steps=2)
+    m = engine.map(8, k0, v0)
+    st, _, _, msg = m.evolve(terms, 0.05, 2, options(0.0))
+    assert st == ost == 0, msg
+    k, v = m.download()
+    m.close()
+    assert len(v) > 4096
+    assert np.array_equal(k, ok) and np.array_equal(bits(v), bits(ov))
