@@ -1,0 +1,469 @@
+#!/usr/bin/env python
+"""Pauli terms/s of the device-resident branch step on GB300.
+
+Workload (default): the 64-spin periodic ring with all-pairs secular dipolar
+couplings d = 1/r^3 (r the chord on a unit-spacing circle), observable X_0,
+dt = 0.005, threshold 1e-5, 128-bit keys -- the larger plain-method benchmark
+configuration.  Its full 1000-step trajectory is far too long for one bench
+run, so a bench "step" is one Strang step (12,096 rotations) of a window of
+that trajectory: the map is first evolved from X_0 (untimed set-up) until it
+holds at least --target-terms terms, then W warm-up steps run, then exactly
+K steps are timed.
+
+Metric: Pauli terms/s = (sum over the timed rotations of the rotation's input
+terms) / device time of the K steps (CUDA events on the engine's stream).
+
+Extra keys: e2e (same metric through the C-ABI with host
+buffers: every step uploads the map from pinned host memory, runs the step
+and downloads the result), roofline (HBM bound, the dominant kernel's
+algorithmic bytes per launch over its average launch time, from a profiled
+step), cpu_baseline (the CPU oracle on a bounded sample of the same state),
+clocks (nvidia-smi sampled during the timed region), gpu_launches.
+
+--impl reference times the reference algorithm on the host cores instead
+(the oracle port, or the reference engine itself where it was compiled).
+Multi-GPU: independent replicas (the path has no data-parallel exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from ddevol_gb300 import hamiltonians as H  # noqa: E402
+
+METRIC = "Pauli terms/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+CONFIGS = {
+    "ring64": dict(
+        n=64, dt=0.005, threshold=1e-5,
+        terms=lambda: H.ring_all_pairs(64),
+        init=lambda: H.single_site_operator(64, 0),
+        label="64-spin periodic ring, all-pairs d=1/r^3 (chord), X_0, dt=0.005, "
+              "threshold 1e-5, 128-bit keys"),
+    "ring16": dict(
+        n=16, dt=0.01, threshold=1e-6,
+        terms=lambda: H.ring_j1j2(16),
+        init=lambda: H.single_site_operator(16, 0),
+        label="16-spin periodic ring, J1=1, J2=1/8, X_0, dt=0.01, threshold 1e-6, "
+              "64-bit keys"),
+    "cubic": dict(
+        n=64, dt=0.005, threshold=1e-5,
+        terms=lambda: H.cubic_111(4),
+        init=lambda: H.single_site_operator(64, 0),
+        label="4x4x4 periodic simple cubic, field [111], r<=2, X on site 0, dt=0.005, "
+              "threshold 1e-5, 128-bit keys"),
+}
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def physical_gpu_index(local_rank):
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        items = [v.strip() for v in vis.split(",") if v.strip()]
+        if local_rank < len(items) and items[local_rank].isdigit():
+            return int(items[local_rank])
+    return local_rank
+
+
+# ------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local_rank)
+            dist.init_process_group("nccl")
+            self.dist = dist
+            self.torch = torch
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            self.dist.barrier()
+
+    def reduce(self, value, op="max"):
+        if not self.pg:
+            return value
+        t = self.torch.tensor([float(value)], dtype=self.torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.dist.destroy_process_group()
+
+
+# ------------------------------------------------------------- CPU samples
+def cpu_sample(keys, vals, n, terms, dt, threshold, budget_s, cores):
+    """Rotations of one Strang step (forward order) on the CPU oracle, from the
+    given state, until the wall budget is spent.  Returns (terms, seconds,
+    rotations, kind)."""
+    half = dt * 0.5
+    impl, kind = None, "port"
+    ref_so = os.path.join(ROOT, "oracle", "_ref", "libtpgp_ref.so")
+    from oracle.oracle import Oracle
+    impl = Oracle()
+    if os.path.exists(ref_so):
+        try:
+            from oracle.oracle import Reference
+            ref = Reference(ref_so)
+            kind = "reference"
+        except OSError:
+            ref = None
+    else:
+        ref = None
+    done_terms, rot = 0, 0
+    k, v = keys, vals
+    t0 = time.perf_counter()
+    order = list(terms) + list(reversed(terms))
+    while rot < len(order):
+        i, j, qi, qj, h = order[rot]
+        n_in = len(v)
+        if ref is not None:
+            # the reference engine, OpenMP backend, all cores (tpgp_rev.c:668-678)
+            st, k, v, _ = ref.rotate(k, v, n, i, j, qi, qj, h * half, threshold=threshold,
+                                     threads=cores, backend=2)
+        else:
+            st, k, v, _ = impl.rotate(k, v, n, i, j, qi, qj, h, half, threshold=threshold,
+                                      threads=cores)
+        if st:
+            raise RuntimeError(f"CPU sample rotation failed with status {st}")
+        done_terms += n_in
+        rot += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return done_terms, time.perf_counter() - t0, rot, kind
+
+
+# ------------------------------------------------------------------ set-up
+def prepare_state(eng, cfg, target_terms, max_setup_steps, opts):
+    terms = cfg["terms"]()
+    k0, v0 = cfg["init"]()
+    m = eng.map(cfg["n"], k0, v0)
+    from ddevol_gb300.engine import GbLedger
+    led = GbLedger()
+    steps = 0
+    while len(m) < target_terms and steps < max_setup_steps:
+        chunk = 1 if len(m) > target_terms / 4 else 4
+        st, _, led, msg = m.evolve(terms, cfg["dt"], chunk, opts, led, record_fid=False)
+        if st:
+            raise RuntimeError(f"set-up evolve failed: {msg}")
+        steps += chunk
+    return m, terms, led, steps
+
+
+def algorithmic_bytes(words, n_in_sum, n_out_sum):
+    return (8 * words + 8) * (n_in_sum + n_out_sum)
+
+
+def read_traffic_profile(kernel, cfg_name):
+    """Per-input-term DRAM bytes of `kernel` from the committed ncu summary
+    (profiles/<kernel>_<config>.md, line 'dram_bytes_per_input_term: X')."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{cfg_name}.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("dram_bytes_per_input_term:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        return None
+    return None
+
+
+def run_gb300(args, dist):
+    from ddevol_gb300.engine import Engine, options
+    cfg = CONFIGS[args.config]
+    words = (cfg["n"] + 31) // 32
+    eng = Engine(dist.local_rank)
+    opts = options(cfg["threshold"], exact_ledger=args.exact_ledger, use_graphs=True)
+    m, terms, led, setup_steps = prepare_state(eng, cfg, args.target_terms, args.max_setup_steps,
+                                               opts)
+    n_start_window = len(m)
+    for _ in range(args.warmup):
+        st, _, led, msg = m.evolve(terms, cfg["dt"], 1, opts, led)
+        if st:
+            raise RuntimeError(msg)
+    # ---- timed region: exactly K steps
+    sampler = ClockSampler(physical_gpu_index(dist.local_rank))
+    sampler.start()
+    time.sleep(0.3)
+    n_before = len(m)
+    dist.barrier()
+    st, fids, led, msg = m.evolve(terms, cfg["dt"], args.steps, opts, led)
+    if st:
+        raise RuntimeError(msg)
+    dist.barrier()
+    ms = m.last_elapsed_ms()
+    terms_done = m.last_terms()
+    launches = m.last_launches()
+    n_after = len(m)
+    clocks = sampler.stop()
+    t_max = dist.reduce(ms / 1e3, "max")
+    terms_all = dist.reduce(float(terms_done), "sum")
+    value = terms_all / t_max
+
+    # ---- profiled step (per-kernel CUDA events) for the roofline
+    m.set_profiling(True)
+    n_p0 = len(m)
+    st, _, led, msg = m.evolve(terms, cfg["dt"], 1, opts, led, record_fid=False)
+    prof = m.kernel_profile()
+    prof_terms = m.last_terms()
+    n_p1 = len(m)
+    m.set_profiling(False)
+    rot = prof["k_merge"][1] or 1
+    total_ms = sum(v[0] for v in prof.values())
+    dominant = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dominant]
+    n_in_sum = prof_terms
+    n_out_sum = prof_terms + (n_p1 - n_p0)
+    bytes_per_launch = algorithmic_bytes(words, n_in_sum, n_out_sum) / rot
+    peak, peak_kind = peaks()
+    achieved = bytes_per_launch / (dom_ms / dom_n / 1e3) / 1e9
+    path_achieved = algorithmic_bytes(words, n_in_sum, n_out_sum) / (total_ms / 1e3) / 1e9
+    traffic_per_term = read_traffic_profile(dominant, args.config)
+    traffic = None if traffic_per_term is None else traffic_per_term * (n_in_sum / rot)
+
+    # ---- end to end through the C-ABI with pinned host buffers
+    e2e = None
+    try:
+        import torch
+        cap = int(len(m) * 1.6) + 4096
+        hk = torch.empty(cap * words, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        hv = torch.empty(cap, dtype=torch.float64, pin_memory=True).numpy()
+        k, v = m.download()
+        hk[:len(k)] = k
+        hv[:len(v)] = v
+        n_host = len(v)
+        e2e_terms, e2e_s, h2d, d2h = 0, 0.0, 0, 0
+        e2e_steps = max(1, min(args.steps, 2))
+        dist.barrier()
+        for _ in range(e2e_steps):
+            t0 = time.perf_counter()
+            st, msg = m.upload(hk[:n_host * words], hv[:n_host])
+            if st:
+                raise RuntimeError(msg)
+            st, led, msg = m.strang_step(terms, cfg["dt"], opts, led)
+            if st:
+                raise RuntimeError(msg)
+            n_new = len(m)
+            if n_new > cap:
+                raise RuntimeError("e2e host buffer too small")
+            from ddevol_gb300.engine import _f64p, _u64p
+            import ctypes as C
+            got = C.c_size_t()
+            err = C.create_string_buffer(256)
+            st = m.lib.tpgp_gb_map_download(m.ptr, _u64p(hk), _f64p(hv), cap, C.byref(got), err,
+                                            256)
+            if st:
+                raise RuntimeError(err.value.decode())
+            e2e_s += time.perf_counter() - t0
+            e2e_terms += m.last_terms()
+            h2d += n_host * (8 * words + 8)
+            d2h += got.value * (8 * words + 8)
+            n_host = got.value
+        dist.barrier()
+        e2e_t = dist.reduce(e2e_s, "max")
+        e2e_all = dist.reduce(float(e2e_terms), "sum")
+        e2e = {"value": e2e_all / e2e_t, "unit": METRIC, "h2d_bytes_per_step": h2d // e2e_steps,
+               "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps}
+    except Exception as exc:  # reported, never silently replaced
+        e2e = {"value": None, "unit": METRIC, "error": str(exc)[:200]}
+
+    # ---- CPU baseline on a bounded sample of the same state (rank 0, N=1)
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        k, v = m.download()
+        cores = os.cpu_count() or 1
+        t_terms, secs, rots, kind = cpu_sample(k, v, cfg["n"], terms, cfg["dt"], cfg["threshold"],
+                                               args.cpu_budget, cores)
+        cpu = {"value": t_terms / secs, "unit": METRIC, "cores": cores, "kind": kind,
+               "sample": f"first {rots} rotations of one Strang step from the {len(v)}-term "
+                         f"window state ({t_terms} input terms, {secs:.1f} s)"}
+    m.close()
+    eng.close()
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (trajectory generated from X_0; no dataset)",
+        "config": {
+            "workload": f"{args.config}_trajectory_window", "description": cfg["label"],
+            "n_spins": cfg["n"], "key_words": words, "hamiltonian_terms": len(terms),
+            "rotations_per_step": 2 * len(terms), "setup_steps": setup_steps,
+            "window_start_step": setup_steps + args.warmup,
+            "terms_at_window_start": n_before, "terms_after_window": n_after,
+            "ledger": "exact (sequential)" if args.exact_ledger else "bound (tree)",
+            "l2": f"map {n_before * (8 * words + 8) / 1e6:.0f} MB per buffer; no flush "
+                  f"(L2 129 MB)",
+            "parallelism": f"replicas x{dist.world}"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "roofline": {
+            "bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "bytes_per_launch": bytes_per_launch, "launch_ms": dom_ms / dom_n,
+            "kernel_share": dom_ms / total_ms,
+            "path_achieved": path_achieved, "path_frac": path_achieved / peak,
+            "kernel_ms": {k2: round(v2[0], 3) for k2, v2 in prof.items()}},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "fid_last": float(fids[-1]) if len(fids) else None,
+    }
+    return line
+
+
+def run_reference(args, dist):
+    """The reference algorithm on the host cores, on samples of the same state."""
+    if dist.rank != 0:
+        return None
+    from ddevol_gb300.engine import Engine, options
+    cfg = CONFIGS[args.config]
+    words = (cfg["n"] + 31) // 32
+    # set-up only: the window-start state comes from the device engine (untimed)
+    eng = Engine(dist.local_rank)
+    opts = options(cfg["threshold"], exact_ledger=True)
+    m, terms, _, setup_steps = prepare_state(eng, cfg, args.target_terms, args.max_setup_steps,
+                                             opts)
+    k, v = m.download()
+    m.close()
+    eng.close()
+    cores = os.cpu_count() or 1
+    budget = max(2.0, args.cpu_budget / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_sample(k, v, cfg["n"], terms, cfg["dt"], cfg["threshold"], min(budget, 2.0), cores)
+    tot_terms, tot_s, tot_rot, kind = 0, 0.0, 0, "port"
+    for _ in range(args.steps):
+        t_terms, secs, rots, kind = cpu_sample(k, v, cfg["n"], terms, cfg["dt"], cfg["threshold"],
+                                               budget, cores)
+        tot_terms += t_terms
+        tot_s += secs
+        tot_rot += rots
+    value = tot_terms / tot_s
+    sample = (f"{args.steps} samples of the first rotations of one Strang step from the "
+              f"{len(v)}-term window state ({tot_rot} rotations, {tot_terms} input terms)")
+    return {
+        "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (trajectory generated from X_0; no dataset)",
+        "config": {"workload": f"{args.config}_trajectory_window", "description": cfg["label"],
+                   "n_spins": cfg["n"], "key_words": words, "setup_steps": setup_steps,
+                   "terms_at_window_start": len(v), "parallelism": "host cores"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="ring64")
+    ap.add_argument("--target-terms", type=float, default=4e6)
+    ap.add_argument("--max-setup-steps", type=int, default=400)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--exact-ledger", action="store_true",
+                    help="bitwise reference ledger (one sequential sum per rotation)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    dist = Dist()
+    try:
+        line = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
+    finally:
+        dist.close()
+    if line is not None and dist.rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -228,6 +228,7 @@ struct DeviceState {
     unsigned int p1_counter, p3_counter, pad0;
     unsigned long long p1_tiles, p3_tiles;  // tiles used (cleared by the commit kernel)
     unsigned long long rotations_done;      // rotations committed in the current call
+    unsigned long long terms_in;            // input terms of the committed rotations
     Ledger ledger;
 };
 

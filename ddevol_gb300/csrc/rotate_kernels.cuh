@@ -777,6 +777,7 @@ __global__ void __launch_bounds__(kCommitBlock) k_commit(RotParams p, Buffers b)
                 st->ledger = next;
                 st->n = n_out;
                 st->rotations_done += 1;
+                st->terms_in += n;
             }
         }
     } else if (!status && threadIdx.x == 0) {

@@ -206,6 +206,20 @@ class DeviceMap:
     def last_launches(self):
         return self.lib.tpgp_gb_last_launches(self.ptr)
 
+    def last_terms(self):
+        return self.lib.tpgp_gb_last_terms(self.ptr)
+
+    KERNELS = ("k_classify", "k_flip_sort", "k_partition", "k_merge", "k_commit")
+
+    def set_profiling(self, on=True):
+        self.lib.tpgp_gb_set_profiling(self.ptr, int(bool(on)))
+
+    def kernel_profile(self):
+        ms = (C.c_double * 5)()
+        n = (C.c_size_t * 5)()
+        self.lib.tpgp_gb_kernel_profile(self.ptr, ms, n)
+        return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNELS)}
+
     def close(self):
         if getattr(self, "ptr", None):
             self.lib.tpgp_gb_map_destroy(self.ptr)

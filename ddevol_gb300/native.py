@@ -92,6 +92,10 @@ def _bind(lib):
     lib.tpgp_gb_last_elapsed_ms.argtypes = [C.c_void_p]
     lib.tpgp_gb_last_launches.restype = sz
     lib.tpgp_gb_last_launches.argtypes = [C.c_void_p]
+    lib.tpgp_gb_last_terms.restype = sz
+    lib.tpgp_gb_last_terms.argtypes = [C.c_void_p]
+    lib.tpgp_gb_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    lib.tpgp_gb_kernel_profile.argtypes = [C.c_void_p, f64p, P(sz)]
     return lib
 
 

@@ -134,11 +134,25 @@ tpgp_gb_status tpgp_gb_evolve(tpgp_gb_map *map, const tpgp_gb_term *terms, size_
  * (engine/include/tpgp_rev.h:73, engine/src/tpgp_rev.c:311-338). */
 tpgp_gb_status tpgp_gb_single_sum(const tpgp_gb_map *map, unsigned pauli, double *sum);
 
-/* Device time of the last rotation kernels, for measurement: the summed
- * duration (ms) of the most recent tpgp_gb_strang_step / tpgp_gb_evolve
- * call's timed region, and the number of kernel launches it issued. */
+/* Measurement of the most recent tpgp_gb_rotate / tpgp_gb_strang_step /
+ * tpgp_gb_evolve call (no reference counterpart; the reference CLI records
+ * only wall seconds, engine/src/cli_rev.c:572-608):
+ *   last_elapsed_ms: device time (CUDA events on the map's stream) from the
+ *     call's first launch to its last completion, host gaps included;
+ *   last_launches:   kernels launched by the call;
+ *   last_terms:      input terms summed over the call's committed rotations
+ *                    (the Pauli terms/s numerator). */
 double tpgp_gb_last_elapsed_ms(const tpgp_gb_map *map);
 size_t tpgp_gb_last_launches(const tpgp_gb_map *map);
+size_t tpgp_gb_last_terms(const tpgp_gb_map *map);
+
+/* Per-kernel profile (no reference counterpart).  With profiling on, the
+ * next calls launch without graphs and bracket every kernel with CUDA
+ * events; kernel_profile then reports, for the five rotation kernels in
+ * pipeline order (classify, flip-sort, partition, merge, commit), the summed
+ * device milliseconds and launch counts since profiling was switched on. */
+void tpgp_gb_set_profiling(tpgp_gb_map *map, int on);
+void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t *launches);
 
 #ifdef __cplusplus
 }
