@@ -224,8 +224,9 @@ struct DeviceState {
     unsigned long long a;        // anticommuting terms of the current rotation
     unsigned long long n_out;    // terms kept by the current rotation
     unsigned long long removed;  // terms removed by the threshold in the current rotation
+    unsigned long long a_next;   // anticommuting terms of the next rotation (set by k_merge)
     unsigned int status;         // sticky ST_* bits
-    unsigned int p1_counter, p3_counter, pad0;
+    unsigned int p1_counter, p3_counter, merge_done;
     unsigned long long p1_tiles, p3_tiles;  // tiles used (cleared by the commit kernel)
     unsigned long long rotations_done;      // rotations committed in the current call
     unsigned long long terms_in;            // input terms of the committed rotations

@@ -32,10 +32,12 @@
 //   k_partition : merge-path split points between the cos list and the
 //                 sorted flipped list, never separating a key pair   [P3a]
 //   k_merge     : merge, combine each key pair, drop zeros, threshold,
-//                 look-back compaction of kept terms (and of removed ones for
-//                 the exact ledger), per-tile ledger partial sums     [P3b]
-//   k_commit    : ledger update, cap and budget checks, state for the next
-//                 rotation                                            [commit]
+//                 look-back compaction of the kept terms, per-tile ledger
+//                 partial sums, and the next rotation's classification of
+//                 every kept term (its flipped children go straight to the
+//                 next k_flip_sort); the last CTA commits the rotation:
+//                 ledger update, cap and budget checks             [P3b+P1']
+// k_classify runs only for the first rotation of a call.
 #pragma once
 #include "common.cuh"
 
@@ -56,6 +58,12 @@ struct RotParams {
     int exact_ledger;       // 1: removed values kept in order for a sequential ledger
     unsigned long long max_terms;
     double max_drop_l2;
+    // the next rotation's generator, classified inside this rotation's merge
+    int has_next;
+    int n_i_word, n_i_shift, n_j_word, n_j_shift;
+    unsigned n_qi, n_qj;
+    double n_s;
+    uint64_t n_mask[4];
 };
 
 struct Buffers {
@@ -67,7 +75,8 @@ struct Buffers {
     double* fv;
     uint64_t* sk;                  // flipped children, key order
     double* sv;
-    double* rem;                   // removed |v| in key order (exact ledger)
+    double* rem;                   // removed |v|, per merge tile in key order (exact ledger)
+    unsigned* rem_count;           // removed terms per merge tile
     unsigned long long* splits;    // merge-path split (i, j) per tile boundary
     double* partials;              // per-tile (l1, sq) partial ledger sums
     unsigned long long* p1_tiles;  // look-back words
@@ -77,8 +86,11 @@ struct Buffers {
 };
 
 constexpr int kP1Block = 256, kP1Items = 8, kP1Tile = kP1Block * kP1Items;
-constexpr int kP2Block = 256, kP2Items = 8, kP2Tile = kP2Block * kP2Items;
-constexpr int kP3Block = 256, kP3Items = 8, kP3Tile = kP3Block * kP3Items;
+// An odd number of items per thread keeps the blocked shared-memory accesses
+// (thread t reads elements t*I .. t*I+I-1) free of bank conflicts for
+// one-word keys (stride 56 B) and at most 2-way for two-word keys.
+constexpr int kP2Block = 256, kP2Items = 7, kP2Tile = kP2Block * kP2Items;
+constexpr int kP3Block = 256, kP3Items = 7, kP3Tile = kP3Block * kP3Items;
 constexpr int kCommitBlock = 1024;
 constexpr int kBlInf = 0x7fff;  // digit-boundary level of element 0
 static_assert(kP1Items * (kP1Block / 32) == 64, "P1 row/warp scan assumes 64 entries");
@@ -116,6 +128,7 @@ __global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
     if (st->status) return;
     const unsigned long long n = st->n;
     const unsigned long long ntiles = (n + kP1Tile - 1) / kP1Tile;
+    if (blockIdx.x >= ntiles) return;  // never needed: fewer tiles than CTAs
     const Key<W> M = mask_key<W>(p);
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     for (;;) {
@@ -442,35 +455,176 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
 }
 
 // ====================================================================== P3a
+// One warp per tile boundary: a 32-ary search along the merge-path diagonal
+// (each round the 32 lanes probe 32 evenly spaced positions in parallel), so
+// a split costs ~log_32(n) dependent memory round trips instead of log_2(n).
 template <int W>
 __global__ void k_partition(RotParams p, Buffers b) {
     DeviceState* st = b.st;
     if (st->status) return;
     const unsigned long long n = st->n, a = st->a, L = n + a;
     const unsigned long long ntiles = (L + kP3Tile - 1) / kP3Tile;
-    for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-         t <= ntiles; t += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned lane = lane_id();
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    for (unsigned long long t = (unsigned long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+         t <= ntiles; t += warps) {
         const unsigned long long d = min(t * (unsigned long long)kP3Tile, L);
+        // smallest i in [lo, hi] with K[i] merged after S[d-i-1] (ties: cos list first)
         unsigned long long lo = d > a ? d - a : 0, hi = min(d, n);
-        while (lo < hi) {
-            const unsigned long long mid = lo + (hi - lo) / 2;
-            // is K[mid] merged before S[d - mid - 1]?  (ties: cos list first)
-            if (key_le<W>(load_key<W>(b.in_keys, mid), load_key<W>(b.sk, d - mid - 1)))
-                lo = mid + 1;
-            else
-                hi = mid;
+        while (hi > lo) {
+            const unsigned long long span = hi - lo;
+            const unsigned long long step = span <= 32 ? 1 : (span + 31) / 32;
+            const unsigned long long probe = lo + (unsigned long long)(lane + 1) * step - 1;
+            bool before = false;
+            if (probe < hi)
+                before = key_le<W>(load_key<W>(b.in_keys, probe), load_key<W>(b.sk, d - probe - 1));
+            const unsigned c = __popc(__ballot_sync(0xffffffffu, before));
+            const unsigned long long new_lo = lo + (unsigned long long)c * step;
+            const unsigned long long new_hi = min(hi, lo + (unsigned long long)(c + 1) * step - 1);
+            if (step == 1) {
+                lo = new_lo;
+                break;
+            }
+            lo = new_lo;
+            hi = max(new_lo, new_hi);
         }
-        unsigned long long i = lo, j = d - lo;
-        // keep a (cos, sin) pair with equal keys inside one tile
-        if (i > 0 && j < a && key_eq<W>(load_key<W>(b.in_keys, i - 1), load_key<W>(b.sk, j))) ++j;
-        b.splits[2 * t] = i;
-        b.splits[2 * t + 1] = j;
+        if (lane == 0) {
+            unsigned long long i = lo, j = d - lo;
+            // keep a (cos, sin) pair with equal keys inside one tile
+            if (i > 0 && j < a && key_eq<W>(load_key<W>(b.in_keys, i - 1), load_key<W>(b.sk, j))) ++j;
+            b.splits[2 * t] = i;
+            b.splits[2 * t + 1] = j;
+        }
     }
 }
 
 // ====================================================================== P3b
+// Merge + combine + threshold + compaction of rotation r, fused with the
+// classification of rotation r+1 (when p.has_next): every kept output term
+// is tested against the next generator and, if it anticommutes, its flipped
+// child is written straight into fk/fv for the next rotation's k_flip_sort,
+// so the map is read once per rotation.  The look-back word carries
+// (kept, next-anticommuting) counts.  The last CTA to finish commits the
+// rotation (ledger, cap, budget) and resets the per-rotation state.
+
+// Ledger update of tpgp_rev.c:730-753 (non-validated) by one CTA, then the
+// per-rotation reset.  Fields written by other CTAs are read with __ldcg.
+template <int NT>
+__device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned long long ntiles) {
+    constexpr int NW = NT / 32;
+    constexpr unsigned long long T = kP3Tile + 1;
+    __shared__ double c_l1[NW], c_sq[NW];
+    __shared__ unsigned long long c_n, c_a;
+    __shared__ unsigned c_status;
+    DeviceState* st = b.st;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        c_status = __ldcg(&st->status);
+        c_n = __ldcg(&st->n);
+        c_a = __ldcg(&st->a);
+    }
+    __syncthreads();
+    const unsigned status = c_status;
+    const unsigned long long n = c_n;
+    double l1 = 0.0, sq = 0.0;
+    if (!status && n > 0) {
+        if (p.exact_ledger) {
+            // the reference's sequential order: key order = tile order, one thread
+            if (threadIdx.x == 0) {
+                for (unsigned long long t = 0; t < ntiles; ++t) {
+                    const unsigned cnt = __ldcg(b.rem_count + t);
+                    const double* r = b.rem + t * T;
+                    for (unsigned k = 0; k < cnt; ++k) {
+                        const double v = __ldcg(r + k);
+                        l1 = up_add(l1, v);
+                        sq = up_add(sq, up_mul(v, v));
+                    }
+                }
+            }
+        } else {
+            // deterministic fixed-shape tree over the per-tile partials
+            const unsigned long long per = (ntiles + NT - 1) / NT;
+            const unsigned long long lo = threadIdx.x * per;
+            const unsigned long long hi = min(ntiles, lo + per);
+            for (unsigned long long t = lo; t < hi; ++t) {
+                l1 = up_add(l1, __ldcg(b.partials + 2 * t));
+                sq = up_add(sq, __ldcg(b.partials + 2 * t + 1));
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const double o1 = __shfl_down_sync(0xffffffffu, l1, off);
+                const double o2 = __shfl_down_sync(0xffffffffu, sq, off);
+                l1 = up_add(l1, o1);
+                sq = up_add(sq, o2);
+            }
+            if (lane == 0) {
+                c_l1[warp] = l1;
+                c_sq[warp] = sq;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                l1 = 0.0;
+                sq = 0.0;
+                for (int w = 0; w < NW; ++w) {
+                    l1 = up_add(l1, c_l1[w]);
+                    sq = up_add(sq, c_sq[w]);
+                }
+            }
+        }
+        if (threadIdx.x == 0) {
+            const unsigned long long n_out = __ldcg(&st->n_out);
+            const unsigned long long removed = __ldcg(&st->removed);
+            unsigned fail = 0;
+            if (p.max_terms && n_out > p.max_terms) fail = ST_CAP;
+            Ledger next = st->ledger;
+            if (!fail) {
+                const double l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
+                next.dropped_l1 = up_add(next.dropped_l1, l1);
+                next.dropped_l2 = up_add(next.dropped_l2, l2);
+                next.dropped_l2_squared = up_add(next.dropped_l2_squared, sq);
+                next.arithmetic_l2 = up_add(next.arithmetic_l2, 0.0);
+                next.rotations += 1;
+                if (removed) next.removal_events += 1;
+                if (n_out > next.peak_terms) next.peak_terms = n_out;
+                next.arithmetic_enclosed = 0;
+                if (!is_finite(next.dropped_l2) || !is_finite(next.arithmetic_l2)) fail = ST_NUMERIC;
+                else if (p.max_drop_l2 != 0.0 && next.dropped_l2 > p.max_drop_l2) fail = ST_BUDGET;
+            }
+            if (fail) {
+                atomicOr(&st->status, fail);
+            } else {
+                st->ledger = next;
+                st->n = n_out;
+                st->a = p.has_next ? __ldcg(&st->a_next) : 0;
+                st->rotations_done += 1;
+                st->terms_in += n;
+            }
+        }
+    } else if (!status && threadIdx.x == 0) {
+        st->rotations_done += 1;  // empty map: a no-op rotation, no ledger change
+        st->a = 0;
+    }
+    __syncthreads();
+    // clear the look-back words this rotation used (clamped to the arrays)
+    const unsigned long long t1_max = (b.cap + kP1Tile - 1) / kP1Tile;
+    const unsigned long long t3_max = (b.cap + kP3Tile - 1) / kP3Tile;
+    const unsigned long long t1 = min((n + kP1Tile - 1) / kP1Tile, t1_max);
+    const unsigned long long t3 = min(ntiles, t3_max);
+    for (unsigned long long t = threadIdx.x; t <= t1; t += NT) b.p1_tiles[t] = 0;
+    for (unsigned long long t = threadIdx.x; t <= t3; t += NT) b.p3_tiles[t] = 0;
+    if (threadIdx.x == 0) {
+        st->p1_counter = 0;
+        st->p3_counter = 0;
+        st->merge_done = 0;
+        st->n_out = 0;
+        st->removed = 0;
+        st->a_next = 0;
+    }
+    (void)c_a;
+}
+
 template <int W>
-__global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
+__global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
     constexpr int T = kP3Tile + 1;  // one extra slot for a pair moved across the boundary
     constexpr int NW = kP3Block / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -478,17 +632,23 @@ __global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
     uint64_t* s_fk = s_kk + (size_t)T * W;                        // sorted flipped keys
     double* s_kv = reinterpret_cast<double*>(s_fk + (size_t)T * W);
     double* s_fv = s_kv + T;
-    unsigned* s_src = reinterpret_cast<unsigned*>(s_fv + T);      // merged order
-    __shared__ unsigned long long s_tile, s_base_k, s_base_r;
-    __shared__ unsigned s_wk[NW], s_wr[NW];
+    __shared__ unsigned long long s_tile, s_base_k, s_base_n;
+    __shared__ unsigned s_wk[NW], s_wn[NW], s_wr[NW];
     __shared__ double s_l1[NW], s_sq[NW];
+    __shared__ int s_last;
 
     DeviceState* st = b.st;
     if (st->status) return;
     const unsigned long long n = st->n, a = st->a, L = n + a;
     const unsigned long long ntiles = (L + kP3Tile - 1) / kP3Tile;
+    const unsigned long long participants =
+        max(1ull, min((unsigned long long)gridDim.x, ntiles));
+    if (blockIdx.x >= participants) return;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const double c = p.c;
+    Key<W> MN;
+#pragma unroll
+    for (int w = 0; w < W; ++w) MN.w[w] = p.n_mask[w];
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_tile = atomicAdd(&st->p3_counter, 1u);
@@ -532,9 +692,13 @@ __global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
             for (int w = 0; w < W; ++w) k.w[w] = s_fk[(size_t)e * W + w];
             return k;
         };
-        // each thread merges its own output range [lo, hi)
+        // each thread merges its own output range [lo_d, hi_d) in registers:
+        // merge-path split in shared memory, then a serial merge where a cos
+        // child absorbs its sin partner (the next merged element, equal key)
+        // and a sin child that follows its partner is skipped
         const int lo_d = min(len, (int)threadIdx.x * kP3Items);
         const int hi_d = threadIdx.x == kP3Block - 1 ? len : min(len, lo_d + kP3Items);
+        int ik, jf;
         {
             int lo = max(0, lo_d - nf), hi = min(lo_d, nk);
             while (lo < hi) {
@@ -542,53 +706,47 @@ __global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
                 if (key_le<W>(kkey(mid), fkey(lo_d - mid - 1))) lo = mid + 1;
                 else hi = mid;
             }
-            int ik = lo, jf = lo_d - lo;
-            for (int d = lo_d; d < hi_d; ++d) {
-                bool take_k;
-                if (ik >= nk) take_k = false;
-                else if (jf >= nf) take_k = true;
-                else take_k = key_le<W>(kkey(ik), fkey(jf));
-                s_src[d] = take_k ? (unsigned)ik++ : (0x80000000u | (unsigned)jf++);
-            }
+            ik = lo;
+            jf = lo_d - lo;
         }
-        __syncthreads();
-        // classify: 0 drop, 1 keep, 2 removed
+        // classify: 0 drop, 1 keep, 2 removed; nx: kept and anticommuting with the next generator
         constexpr int MAXI = kP3Items + 1;
+        unsigned short osrc[MAXI];  // tile-local source: K index, or F index | 0x8000
         double val[MAXI];
-        unsigned char cls[MAXI];
-        unsigned cnt_k = 0, cnt_r = 0;
+        unsigned char cls[MAXI], nx[MAXI];
+        unsigned cnt_k = 0, cnt_n = 0, cnt_r = 0;
         double l1 = 0.0, sq = 0.0;
         bool bad = false;
 #pragma unroll
         for (int e = 0; e < MAXI; ++e) {
-            const int d = lo_d + e;
             cls[e] = 0;
+            nx[e] = 0;
             val[e] = 0.0;
-            if (d >= hi_d) continue;
-            const unsigned s = s_src[d];
+            osrc[e] = 0;
+            if (lo_d + e >= hi_d) continue;
+            bool take_k;
+            if (ik >= nk) take_k = false;
+            else if (jf >= nf) take_k = true;
+            else take_k = key_le<W>(kkey(ik), fkey(jf));
             Key<W> key;
             double v;
-            if (s & 0x80000000u) {
-                const int f = (int)(s & 0x7fffffffu);
-                key = fkey(f);
-                if (d > 0) {
-                    const unsigned sp = s_src[d - 1];
-                    // partner of the preceding cos child: already summed there
-                    if (!(sp & 0x80000000u) && key_eq<W>(kkey((int)sp), key)) continue;
-                }
-                v = s_fv[f];
-            } else {
-                const int k = (int)s;
-                key = kkey(k);
-                const double vin = s_kv[k];
+            if (take_k) {
+                key = kkey(ik);
+                osrc[e] = (unsigned short)ik;
+                const double vin = s_kv[ik];
+                ++ik;
                 bool anti, plus;
                 branch_info(p, word_at<W>(key, p.i_word), word_at<W>(key, p.j_word), anti, plus);
                 v = anti ? __dmul_rn(vin, c) : __dadd_rn(vin, 0.0);
-                if (d + 1 < len) {
-                    const unsigned sn = s_src[d + 1];
-                    if ((sn & 0x80000000u) && key_eq<W>(fkey((int)(sn & 0x7fffffffu)), key))
-                        v = __dadd_rn(v, s_fv[sn & 0x7fffffffu]);
-                }
+                // the partner (if any) is the next merged element: sum it here
+                if (jf < nf && key_eq<W>(fkey(jf), key)) v = __dadd_rn(v, s_fv[jf]);
+            } else {
+                key = fkey(jf);
+                osrc[e] = (unsigned short)(0x8000u | (unsigned)jf);
+                v = s_fv[jf];
+                ++jf;
+                // partner of the preceding cos child: already summed there
+                if (ik > 0 && key_eq<W>(kkey(ik - 1), key)) continue;
             }
             if (!is_finite(v)) bad = true;
             if (v == 0.0) continue;  // exact cancellation: dropped, no ledger entry
@@ -596,24 +754,35 @@ __global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
             if (!key_is_zero<W>(key) && fabs(v) <= p.threshold) {
                 cls[e] = 2;
                 ++cnt_r;
-                const double av = fabs(v);
-                l1 = up_add(l1, av);
+                l1 = up_add(l1, fabs(v));
                 sq = up_add(sq, up_mul(v, v));
             } else {
                 cls[e] = 1;
                 ++cnt_k;
+                if (p.has_next) {
+                    const unsigned pi = site_symbol(word_at<W>(key, p.n_i_word), p.n_i_shift);
+                    const unsigned pj = site_symbol(word_at<W>(key, p.n_j_word), p.n_j_shift);
+                    if (anticommutes(p.n_qi, pi) != anticommutes(p.n_qj, pj)) {
+                        const bool plus_n =
+                            ((phase_exponent(p.n_qi, pi) + phase_exponent(p.n_qj, pj)) & 3u) == 1u;
+                        nx[e] = plus_n ? 1 : 2;
+                        ++cnt_n;
+                    }
+                }
             }
         }
         if (bad) atomicOr(&st->status, ST_NUMERIC);
-        // block exclusive scan of (kept, removed) counts in thread order
-        unsigned ik = cnt_k, ir = cnt_r;
+        // block exclusive scans of the three counts in thread order
+        unsigned sk_ = cnt_k, sn_ = cnt_n, sr_ = cnt_r;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            const unsigned tk = __shfl_up_sync(0xffffffffu, ik, off);
-            const unsigned tr = __shfl_up_sync(0xffffffffu, ir, off);
+            const unsigned tk = __shfl_up_sync(0xffffffffu, sk_, off);
+            const unsigned tn = __shfl_up_sync(0xffffffffu, sn_, off);
+            const unsigned tr = __shfl_up_sync(0xffffffffu, sr_, off);
             if (lane >= (unsigned)off) {
-                ik += tk;
-                ir += tr;
+                sk_ += tk;
+                sn_ += tn;
+                sr_ += tr;
             }
         }
         // ledger partials: deterministic tree within the warp, then across warps
@@ -626,31 +795,34 @@ __global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
             wsq = up_add(wsq, o2);
         }
         if (lane == 31) {
-            s_wk[warp] = ik;
-            s_wr[warp] = ir;
+            s_wk[warp] = sk_;
+            s_wn[warp] = sn_;
+            s_wr[warp] = sr_;
         }
         if (lane == 0) {
             s_l1[warp] = wl1;
             s_sq[warp] = wsq;
         }
         __syncthreads();
-        unsigned wk_off = 0, wr_off = 0, tk_tot = 0, tr_tot = 0;
+        unsigned wk_off = 0, wn_off = 0, wr_off = 0, tk_tot = 0, tn_tot = 0, tr_tot = 0;
         for (int w = 0; w < NW; ++w) {
             if (w < (int)warp) {
                 wk_off += s_wk[w];
+                wn_off += s_wn[w];
                 wr_off += s_wr[w];
             }
             tk_tot += s_wk[w];
+            tn_tot += s_wn[w];
             tr_tot += s_wr[w];
         }
         if (warp == 0) {
             const unsigned long long base =
-                lookback_exclusive(b.p3_tiles, tile, pack2(tk_tot, tr_tot), &st->status);
+                lookback_exclusive(b.p3_tiles, tile, pack2(tk_tot, tn_tot), &st->status);
             if (lane == 0) {
-                unsigned long long bk, br;
-                unpack2(base, bk, br);
+                unsigned long long bk, bn;
+                unpack2(base, bk, bn);
                 s_base_k = bk;
-                s_base_r = br;
+                s_base_n = bn;
                 double t1 = 0.0, t2 = 0.0;
                 for (int w = 0; w < NW; ++w) {
                     t1 = up_add(t1, s_l1[w]);
@@ -658,142 +830,59 @@ __global__ void __launch_bounds__(kP3Block) k_merge(RotParams p, Buffers b) {
                 }
                 b.partials[2 * tile] = t1;
                 b.partials[2 * tile + 1] = t2;
+                b.rem_count[tile] = tr_tot;
+                if (tr_tot) atomicAdd(&st->removed, (unsigned long long)tr_tot);
                 if (tile == ntiles - 1) {
-                    st->n_out = bk + tk_tot;
-                    st->removed = br + tr_tot;
-                    st->p3_tiles = ntiles;
+                    const unsigned long long n_out = bk + tk_tot, a_next = bn + tn_tot;
+                    st->n_out = n_out;
+                    st->a_next = a_next;
+                    if (p.has_next && n_out + a_next > b.cap) atomicOr(&st->status, ST_CAPACITY);
                 }
             }
         }
         __syncthreads();
-        unsigned long long ok = s_base_k + wk_off + (ik - cnt_k);
-        unsigned long long orr = s_base_r + wr_off + (ir - cnt_r);
+        unsigned long long ok = s_base_k + wk_off + (sk_ - cnt_k);
+        unsigned long long on = s_base_n + wn_off + (sn_ - cnt_n);
+        unsigned orr = wr_off + (sr_ - cnt_r);
+        const double sn = p.n_s;
 #pragma unroll
         for (int e = 0; e < MAXI; ++e) {
             if (cls[e] == 0) continue;
-            const int d = lo_d + e;
-            const unsigned s = s_src[d];
             if (cls[e] == 1) {
+                const Key<W> key = (osrc[e] & 0x8000u) ? fkey(osrc[e] & 0x7fff) : kkey(osrc[e]);
                 if (ok < b.cap) {
-                    const Key<W> key = (s & 0x80000000u) ? fkey((int)(s & 0x7fffffffu)) : kkey((int)s);
                     store_key<W>(b.out_keys, ok, key);
                     b.out_vals[ok] = val[e];
                 } else {
                     atomicOr(&st->status, ST_CAPACITY);
                 }
                 ++ok;
+                if (nx[e]) {
+                    if (on < b.cap) {
+                        const double y = __dmul_rn(val[e], sn);
+                        store_key<W>(b.fk, on, key_xor<W>(key, MN));
+                        b.fv[on] = nx[e] == 1 ? y : -y;
+                    } else {
+                        atomicOr(&st->status, ST_CAPACITY);
+                    }
+                    ++on;
+                }
             } else {
-                if (p.exact_ledger && orr < b.cap) b.rem[orr] = fabs(val[e]);
+                if (p.exact_ledger) b.rem[tile * (unsigned long long)T + orr] = fabs(val[e]);
                 ++orr;
             }
         }
     }
-}
-
-// =================================================================== commit
-// Ledger update of tpgp_rev.c:730-753 (non-validated), then reset of the
-// per-rotation device state.  One block.
-__global__ void __launch_bounds__(kCommitBlock) k_commit(RotParams p, Buffers b) {
-    __shared__ double s_l1[kCommitBlock / 32], s_sq[kCommitBlock / 32];
-    __shared__ unsigned long long s_n, s_a, s_t1, s_t3;
-    DeviceState* st = b.st;
-    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    // the last CTA to finish commits the rotation
+    __syncthreads();
     if (threadIdx.x == 0) {
-        s_n = st->n;
-        s_a = st->a;
-        // clamp to the look-back arrays (n + a can exceed cap when the
-        // rotation ran out of room)
-        const unsigned long long t1_max = (b.cap + kP1Tile - 1) / kP1Tile;
-        const unsigned long long t3_max = (b.cap + kP3Tile - 1) / kP3Tile;
-        s_t1 = min((s_n + kP1Tile - 1) / kP1Tile, t1_max);
-        s_t3 = min((s_n + s_a + kP3Tile - 1) / kP3Tile, t3_max);
+        __threadfence();
+        s_last = atomicAdd(&st->merge_done, 1u) == (unsigned)(participants - 1);
     }
     __syncthreads();
-    const unsigned status = st->status;
-    const unsigned long long n = s_n;
-    double l1 = 0.0, sq = 0.0;
-    if (!status && n > 0) {
-        const unsigned long long removed = st->removed;
-        if (p.exact_ledger) {
-            // the reference's sequential order: sorted key order, one thread
-            if (threadIdx.x == 0) {
-                for (unsigned long long k = 0; k < removed; ++k) {
-                    const double v = b.rem[k];
-                    l1 = up_add(l1, v);
-                    sq = up_add(sq, up_mul(v, v));
-                }
-            }
-        } else {
-            // deterministic tree over the per-tile partials (fixed shape)
-            const unsigned long long nt = st->p3_tiles;
-            const unsigned long long per = (nt + kCommitBlock - 1) / kCommitBlock;
-            const unsigned long long lo = threadIdx.x * per, hi = min(nt, lo + per);
-            for (unsigned long long t = lo; t < hi; ++t) {
-                l1 = up_add(l1, b.partials[2 * t]);
-                sq = up_add(sq, b.partials[2 * t + 1]);
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const double o1 = __shfl_down_sync(0xffffffffu, l1, off);
-                const double o2 = __shfl_down_sync(0xffffffffu, sq, off);
-                l1 = up_add(l1, o1);
-                sq = up_add(sq, o2);
-            }
-            if (lane == 0) {
-                s_l1[warp] = l1;
-                s_sq[warp] = sq;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                l1 = 0.0;
-                sq = 0.0;
-                for (int w = 0; w < kCommitBlock / 32; ++w) {
-                    l1 = up_add(l1, s_l1[w]);
-                    sq = up_add(sq, s_sq[w]);
-                }
-            }
-        }
-        if (threadIdx.x == 0) {
-            const unsigned long long n_out = st->n_out;
-            unsigned fail = 0;
-            if (p.max_terms && n_out > p.max_terms) fail = ST_CAP;
-            Ledger next = st->ledger;
-            if (!fail) {
-                const double l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
-                next.dropped_l1 = up_add(next.dropped_l1, l1);
-                next.dropped_l2 = up_add(next.dropped_l2, l2);
-                next.dropped_l2_squared = up_add(next.dropped_l2_squared, sq);
-                next.arithmetic_l2 = up_add(next.arithmetic_l2, 0.0);
-                next.rotations += 1;
-                if (removed) next.removal_events += 1;
-                if (n_out > next.peak_terms) next.peak_terms = n_out;
-                next.arithmetic_enclosed = 0;
-                if (!is_finite(next.dropped_l2) || !is_finite(next.arithmetic_l2)) fail = ST_NUMERIC;
-                else if (p.max_drop_l2 != 0.0 && next.dropped_l2 > p.max_drop_l2) fail = ST_BUDGET;
-            }
-            if (fail) {
-                atomicOr(&st->status, fail);
-            } else {
-                st->ledger = next;
-                st->n = n_out;
-                st->rotations_done += 1;
-                st->terms_in += n;
-            }
-        }
-    } else if (!status && threadIdx.x == 0) {
-        st->rotations_done += 1;  // empty map: a no-op rotation, no ledger change
-    }
-    __syncthreads();
-    // reset per-rotation scratch: look-back words and tile counters
-    for (unsigned long long t = threadIdx.x; t < s_t1 + 1; t += kCommitBlock) b.p1_tiles[t] = 0;
-    for (unsigned long long t = threadIdx.x; t < s_t3 + 1; t += kCommitBlock) b.p3_tiles[t] = 0;
-    if (threadIdx.x == 0) {
-        st->p1_counter = 0;
-        st->p3_counter = 0;
-        st->a = 0;
-        st->n_out = 0;
-        st->removed = 0;
-    }
+    if (!s_last) return;
+    __threadfence();
+    commit_rotation<kP3Block>(p, b, ntiles);
 }
 
 }  // namespace tg

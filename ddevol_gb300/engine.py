@@ -209,7 +209,7 @@ class DeviceMap:
     def last_terms(self):
         return self.lib.tpgp_gb_last_terms(self.ptr)
 
-    KERNELS = ("k_classify", "k_flip_sort", "k_partition", "k_merge", "k_commit")
+    KERNELS = ("k_classify", "k_flip_sort", "k_partition", "k_merge", "unused")
 
     def set_profiling(self, on=True):
         self.lib.tpgp_gb_set_profiling(self.ptr, int(bool(on)))
@@ -218,7 +218,7 @@ class DeviceMap:
         ms = (C.c_double * 5)()
         n = (C.c_size_t * 5)()
         self.lib.tpgp_gb_kernel_profile(self.ptr, ms, n)
-        return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNELS)}
+        return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNELS) if k != "unused"}
 
     def close(self):
         if getattr(self, "ptr", None):

@@ -148,9 +148,10 @@ size_t tpgp_gb_last_terms(const tpgp_gb_map *map);
 
 /* Per-kernel profile (no reference counterpart).  With profiling on, the
  * next calls launch without graphs and bracket every kernel with CUDA
- * events; kernel_profile then reports, for the five rotation kernels in
- * pipeline order (classify, flip-sort, partition, merge, commit), the summed
- * device milliseconds and launch counts since profiling was switched on. */
+ * events; kernel_profile then reports, for the rotation kernels in pipeline
+ * order (classify, flip-sort, partition, merge; the fifth slot is unused),
+ * the summed device milliseconds and launch counts since profiling was
+ * switched on. */
 void tpgp_gb_set_profiling(tpgp_gb_map *map, int on);
 void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t *launches);
 
