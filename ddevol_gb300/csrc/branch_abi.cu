@@ -63,7 +63,7 @@ bool ranges_overlap(const void* a, size_t as, const void* b, size_t bs) {
 // rounding radius of the serial engine (engine/src/tpgp_rev.c:37-42).
 __device__ __forceinline__ double rounding_radius(double x) {
     if (!tg::is_finite(x)) return __longlong_as_double(0x7ff0000000000000ll);
-    const double up = tg::next_up(x), down = -tg::next_up(-x);
+    const double up = tg::next_up(x), down = tg::negate(tg::next_up(tg::negate(x)));
     const double a = fabs(__dsub_rn(up, x)), b = fabs(__dsub_rn(x, down));
     return a > b ? a : b;
 }
@@ -127,10 +127,10 @@ __global__ void __launch_bounds__(256)
                 const double x = __dmul_rn(v, c), y = __dmul_rn(v, s);
                 double r0 = 0.0, r1 = 0.0;
                 if (enclose) {
-                    r0 = tg::up_add(tg::up_mul(fabs(v), rc), rounding_radius(x));
-                    r1 = tg::up_add(tg::up_mul(fabs(v), rs), rounding_radius(y));
+                    r0 = tg::up_add(tg::up_mul(tg::abs_of(v), rc), rounding_radius(x));
+                    r1 = tg::up_add(tg::up_mul(tg::abs_of(v), rs), rounding_radius(y));
                 }
-                reinterpret_cast<double2*>(out_values)[k] = make_double2(x, plus ? y : -y);
+                reinterpret_cast<double2*>(out_values)[k] = make_double2(x, plus ? y : tg::negate(y));
                 reinterpret_cast<double2*>(out_radii)[k] = make_double2(r0, r1);
                 if (!tg::is_finite(x) || !tg::is_finite(y) || !tg::is_finite(r0) || !tg::is_finite(r1))
                     flags |= 2u;

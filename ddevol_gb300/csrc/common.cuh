@@ -187,27 +187,126 @@ __device__ __forceinline__ unsigned phase_exponent(unsigned q, unsigned p) {
 }
 
 // ------------------------------------------------- directed rounding helpers
-// Exact successor toward +inf of a binary64 value, including zero and
-// subnormal transitions (the reference's nextafter(x, INFINITY)).
+// GB300 issues binary64 arithmetic at a small fraction of its integer rate,
+// so every exact predicate on a binary64 value (zero test, absolute value,
+// sign flip, comparison of non-negative values, successor) works on the bit
+// pattern with integer instructions; only genuine products and sums use the
+// FP64 pipe.  For non-negative finite doubles the IEEE order equals the
+// unsigned order of their bit patterns.
+constexpr unsigned long long kSignBit = 0x8000000000000000ull;
+constexpr unsigned long long kExpMask = 0x7ff0000000000000ull;
+
+// Register moves the compiler cannot see through, so that sign, absolute
+// value and zero tests on the bit pattern stay integer instructions instead
+// of being folded back into FP64 negate/abs/compare operations.
+__device__ __forceinline__ unsigned long long dbits(double x) {
+    unsigned long long u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+    return u;
+}
+__device__ __forceinline__ double from_bits(unsigned long long u) {
+    double x;
+    asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+    return x;
+}
+__device__ __forceinline__ bool is_zero(double x) { return (dbits(x) << 1) == 0; }
+__device__ __forceinline__ bool is_finite(double x) { return (dbits(x) & kExpMask) != kExpMask; }
+__device__ __forceinline__ unsigned long long abs_bits(double x) { return dbits(x) & ~kSignBit; }
+__device__ __forceinline__ double abs_of(double x) { return from_bits(abs_bits(x)); }
+__device__ __forceinline__ double negate(double x) { return from_bits(dbits(x) ^ kSignBit); }
+
+// Exact successor toward +inf (the reference's nextafter(x, INFINITY)),
+// including zero and subnormal transitions; NaN and +inf are unchanged.
 __device__ __forceinline__ double next_up(double x) {
-    if (x != x || x == __longlong_as_double(0x7ff0000000000000ll)) return x;
-    if (x == 0.0) return __longlong_as_double(1ll);
-    long long bits = __double_as_longlong(x);
-    bits = x > 0 ? bits + 1 : bits - 1;
-    return __longlong_as_double(bits);
+    const unsigned long long u = dbits(x);
+    if ((u << 1) == 0) return from_bits(1ull);             // +-0 -> smallest subnormal
+    if ((u & ~kSignBit) > kExpMask || u == kExpMask) return x;  // NaN, +inf
+    return from_bits((u & kSignBit) ? u - 1 : u + 1);
 }
 // upadd / upmul of engine/src/tpgp_rev.c:25-36.
 __device__ __forceinline__ double up_add(double a, double b) {
-    if (a == 0.0) return b;
-    if (b == 0.0) return a;
+    if (is_zero(a)) return b;
+    if (is_zero(b)) return a;
     return next_up(__dadd_rn(a, b));
 }
 __device__ __forceinline__ double up_mul(double a, double b) {
-    if (a == 0.0 || b == 0.0) return 0.0;
+    if (is_zero(a) || is_zero(b)) return 0.0;
     return next_up(__dmul_rn(a, b));
 }
-__device__ __forceinline__ bool is_finite(double x) {
-    return (__double_as_longlong(x) & 0x7ff0000000000000ll) != 0x7ff0000000000000ll;
+
+// ------------------------------------------------- fixed-point ledger sums
+// Upper bounds on sums of removed |v| and v^2 in 128-bit integer fixed
+// point: each addend is rounded UP to a multiple of 2^unit, the sum is exact
+// (order-independent), and the total is converted to binary64 rounding up.
+// The unit is chosen from the threshold t (removed |v| <= t < 2^et):
+// unit1 = et - 96, unit2 = 2 et - 96, so fewer than 2^31 addends never
+// overflow 127 bits.
+struct U128 {
+    unsigned long long lo, hi;
+};
+__device__ __forceinline__ void u128_add(U128& a, const U128& b) {
+    const unsigned long long lo = a.lo + b.lo;
+    a.hi += b.hi + (lo < a.lo ? 1ull : 0ull);
+    a.lo = lo;
+}
+// ceil(x / 2^q) for a 128-bit x and 0 <= q
+__device__ __forceinline__ U128 u128_shr_ceil(U128 x, int q) {
+    if (q <= 0) return x;
+    if (q >= 128) return U128{(x.lo | x.hi) ? 1ull : 0ull, 0ull};
+    U128 r;
+    unsigned long long lost;
+    if (q >= 64) {
+        lost = x.lo | (q > 64 ? (x.hi << (128 - q)) : 0ull);
+        r.lo = q == 64 ? x.hi : (x.hi >> (q - 64));
+        r.hi = 0;
+    } else {
+        lost = x.lo << (64 - q);
+        r.lo = (x.lo >> q) | (x.hi << (64 - q));
+        r.hi = x.hi >> q;
+    }
+    if (lost) {
+        const U128 one{1ull, 0ull};
+        u128_add(r, one);
+    }
+    return r;
+}
+// m * 2^eb with m the 53-bit significand of |v| (binary64, finite, nonzero)
+__device__ __forceinline__ void split_abs(double v, unsigned long long& m, int& eb) {
+    const unsigned long long a = abs_bits(v);
+    const int be = (int)(a >> 52);
+    m = (a & 0x000fffffffffffffull) | (be ? 0x0010000000000000ull : 0ull);
+    eb = (be ? be : 1) - 1075;
+}
+// ceil(|v| / 2^unit1) and ceil(v^2 / 2^unit2); requires |v| < 2^et
+__device__ __forceinline__ void fixed_terms(double v, int unit1, int unit2, U128& x1, U128& x2) {
+    unsigned long long m;
+    int eb;
+    split_abs(v, m, eb);
+    const int sh = eb - unit1;  // <= 43 because |v| < 2^(unit1 + 96)
+    if (sh >= 0) {
+        x1.lo = sh == 0 ? m : (m << sh);
+        x1.hi = sh == 0 ? 0ull : (sh >= 64 ? 0ull : (m >> (64 - sh)));
+    } else {
+        x1 = u128_shr_ceil(U128{m, 0ull}, -sh);
+    }
+    const U128 sq{m * m, __umul64hi(m, m)};
+    x2 = u128_shr_ceil(sq, unit2 - 2 * eb);  // shift >= 10
+}
+__device__ __forceinline__ U128 shfl_down_u128(const U128& x, int off) {
+    return U128{__shfl_down_sync(0xffffffffu, x.lo, off), __shfl_down_sync(0xffffffffu, x.hi, off)};
+}
+// x * 2^unit rounded up to binary64 (one FP64 scaling per rotation)
+__device__ inline double u128_to_double_up(U128 x, int unit) {
+    if (!(x.lo | x.hi)) return 0.0;
+    const int nb = x.hi ? 128 - __clzll((long long)x.hi) : 64 - __clzll((long long)x.lo);
+    int shift = nb > 53 ? nb - 53 : 0;
+    U128 t = u128_shr_ceil(x, shift);
+    if (t.lo >> 53) {  // rounding carried to 2^53
+        t.lo >>= 1;
+        ++shift;
+    }
+    const double r = ldexp((double)t.lo, unit + shift);
+    return r;
 }
 
 // ----------------------------------------------------------- ledger on device

@@ -49,6 +49,7 @@ struct RotParams {
     unsigned qi, qj;
     double c, s;            // host-computed cos/sin (never evaluated on device)
     double threshold;
+    unsigned long long threshold_bits;  // bit pattern of threshold (>= 0, finite)
     uint64_t mask[4];       // Q's bits: qi at site i, qj at site j
     int nlev;               // number of mask bits (radix digits), 0..4
     int mbit[4];            // mask bit positions, descending
@@ -56,6 +57,7 @@ struct RotParams {
     int th[8];              // threshold bit positions
     int lev_lo[4], lev_hi[4];  // index in th of mbit[l] and mbit[l] + 1
     int exact_ledger;       // 1: removed values kept in order for a sequential ledger
+    int fx_unit1, fx_unit2; // fixed-point units of the bound ledger (see fixed_terms)
     unsigned long long max_terms;
     double max_drop_l2;
     // the next rotation's generator, classified inside this rotation's merge
@@ -78,7 +80,7 @@ struct Buffers {
     double* rem;                   // removed |v|, per merge tile in key order (exact ledger)
     unsigned* rem_count;           // removed terms per merge tile
     unsigned long long* splits;    // merge-path split (i, j) per tile boundary
-    double* partials;              // per-tile (l1, sq) partial ledger sums
+    unsigned long long* partials;  // per-tile fixed-point (l1, sq) sums, 4 words per tile
     unsigned long long* p1_tiles;  // look-back words
     unsigned long long* p3_tiles;
     DeviceState* st;
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
             const double v = __ldg(b.in_vals + k);
             const double y = __dmul_rn(v, p.s);
             store_key<W>(b.fk, x, key_xor<W>(key, M));
-            b.fv[x] = plus[e] ? y : -y;
+            reinterpret_cast<unsigned long long*>(b.fv)[x] = dbits(y) ^ (plus[e] ? 0ull : kSignBit);
         }
     }
 }
@@ -268,14 +270,18 @@ __device__ unsigned long long run_edge(const uint64_t* fk, const Key<W>& M,
     }
 }
 
-template <int W>
+// NT: compile-time bound on the number of digit-boundary thresholds (4 when
+// each site carries one mask bit, 6 otherwise).  Positions inside the kernel
+// are 32-bit and relative to the tile start (a map holds < 2^30 terms).
+template <int W, int NT>
 __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* s_keys = reinterpret_cast<uint64_t*>(smem_raw);                 // [tile][W]
     double* s_vals = reinterpret_cast<double*>(s_keys + (size_t)kP2Tile * W);  // [tile]
     short* s_bl = reinterpret_cast<short*>(s_vals + kP2Tile);                 // [tile]
-    __shared__ long long s_gprev[8], s_gnext[8];
-    __shared__ long long s_wprev[kP2Block / 32][8], s_wnext[kP2Block / 32][8];
+    __shared__ int s_gprev[NT], s_gnext[NT];
+    __shared__ int s_wprev[kP2Block / 32][NT], s_wnext[kP2Block / 32][NT];
+    constexpr int kNone = INT_MIN, kEnd = INT_MAX;
 
     DeviceState* st = b.st;
     if (st->status) return;
@@ -285,6 +291,9 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
     const Key<W> M = mask_key<W>(p);
     const int nth = p.nth;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    int th[NT];
+#pragma unroll
+    for (int q = 0; q < NT; ++q) th[q] = q < nth ? p.th[q] : 0x7fffffff;  // unused: never reached
 
     for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const unsigned long long x0 = tile * kP2Tile;
@@ -297,16 +306,20 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
             for (int w = 0; w < W; ++w) s_keys[(size_t)e * W + w] = k.w[w];
             s_vals[e] = __ldg(b.fv + x0 + e);
         }
-        // run edges outside the tile for every threshold (galloping searches)
+        // run edges outside the tile for every threshold (galloping searches),
+        // as offsets from x0
         if (threadIdx.x < 2 * nth) {
             const int q = threadIdx.x % nth;
             if (threadIdx.x < nth) {
                 // last y < x0 with bl(y) >= th[q]: start of the run holding x0-1
-                s_gprev[q] = x0 == 0 ? -1 : (long long)run_edge<W>(b.fk, M, a, x0 - 1, p.th[q], true);
+                s_gprev[q] = x0 == 0 ? kNone
+                                     : (int)((long long)run_edge<W>(b.fk, M, a, x0 - 1, p.th[q], true) -
+                                             (long long)x0);
             } else {
                 // first y >= x1 with bl(y) >= th[q] (a if none)
-                s_gnext[q] = x1 >= a ? (long long)a
-                                     : (long long)max(x1, run_edge<W>(b.fk, M, a, x1 - 1, p.th[q], false));
+                const unsigned long long g =
+                    x1 >= a ? a : max(x1, run_edge<W>(b.fk, M, a, x1 - 1, p.th[q], false));
+                s_gnext[q] = (int)((long long)g - (long long)x0);
             }
         }
         __syncthreads();
@@ -334,100 +347,100 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
 
         // blocked ownership: thread t owns tile elements [t*I, t*I + I)
         const int e0 = threadIdx.x * kP2Items;
-        long long lprev[8], lnext[8];
+        int lprev[NT], lnext[NT];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            lprev[q] = -1;
-            lnext[q] = LLONG_MAX;
+        for (int q = 0; q < NT; ++q) {
+            lprev[q] = kNone;
+            lnext[q] = kEnd;
         }
+        int blv[kP2Items];
+#pragma unroll
         for (int e = 0; e < kP2Items; ++e) {
             const int te = e0 + e;
-            if (te >= len) break;
-            const int bl = s_bl[te];
+            blv[e] = te < len ? s_bl[te] : -1;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                if (q < nth && bl >= p.th[q]) {
-                    lprev[q] = (long long)(x0 + te);
-                    if (lnext[q] == LLONG_MAX) lnext[q] = (long long)(x0 + te);
+            for (int q = 0; q < NT; ++q) {
+                if (blv[e] >= th[q]) {
+                    lprev[q] = te;
+                    if (lnext[q] == kEnd) lnext[q] = te;
                 }
             }
         }
         // exclusive cross-thread scans: max of earlier threads' last, min of later threads' first
-        long long cprev[8], cnext[8];
+        int cprev[NT], cnext[NT];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            long long incl = lprev[q];
+        for (int q = 0; q < NT; ++q) {
+            int incl = lprev[q];
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
-                const long long t = __shfl_up_sync(0xffffffffu, incl, off);
+                const int t = __shfl_up_sync(0xffffffffu, incl, off);
                 if (lane >= (unsigned)off) incl = max(incl, t);
             }
-            long long excl = __shfl_up_sync(0xffffffffu, incl, 1);
-            if (lane == 0) excl = -1;
+            int excl = __shfl_up_sync(0xffffffffu, incl, 1);
+            if (lane == 0) excl = kNone;
             cprev[q] = excl;
             if (lane == 31) s_wprev[warp][q] = incl;
-            long long rincl = lnext[q];
+            int rincl = lnext[q];
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
-                const long long t = __shfl_down_sync(0xffffffffu, rincl, off);
+                const int t = __shfl_down_sync(0xffffffffu, rincl, off);
                 if (lane + off < 32) rincl = min(rincl, t);
             }
-            long long rexcl = __shfl_down_sync(0xffffffffu, rincl, 1);
-            if (lane == 31) rexcl = LLONG_MAX;
+            int rexcl = __shfl_down_sync(0xffffffffu, rincl, 1);
+            if (lane == 31) rexcl = kEnd;
             cnext[q] = rexcl;
             if (lane == 0) s_wnext[warp][q] = rincl;
         }
         __syncthreads();
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            if (q >= nth) break;
-            long long pv = -1, nv = LLONG_MAX;
+        for (int q = 0; q < NT; ++q) {
+            int pv = kNone, nv = kEnd;
             for (int w = 0; w < (int)warp; ++w) pv = max(pv, s_wprev[w][q]);
             for (int w = (int)warp + 1; w < kP2Block / 32; ++w) nv = min(nv, s_wnext[w][q]);
             cprev[q] = max(cprev[q], pv);
             cnext[q] = min(cnext[q], nv);
-            if (cprev[q] < 0) cprev[q] = s_gprev[q];
-            if (cnext[q] == LLONG_MAX) cnext[q] = s_gnext[q];
+            if (q < nth) {
+                if (cprev[q] == kNone) cprev[q] = s_gprev[q];
+                if (cnext[q] == kEnd) cnext[q] = s_gnext[q];
+            }
         }
-        // forward pass: displacement of the digits that are 1 (move back by n0)
-        long long disp[kP2Items];
+        // digits of each element (original key bit = flipped bit xor 1) and
+        // displacement: forward pass moves 1-digits back by n0, backward
+        // pass moves 0-digits ahead by n1
+        int disp[kP2Items];
         {
-            long long run[8];
+            int run[NT];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) run[q] = cprev[q];
+            for (int q = 0; q < NT; ++q) run[q] = cprev[q];
+#pragma unroll
             for (int e = 0; e < kP2Items; ++e) {
                 const int te = e0 + e;
                 disp[e] = 0;
                 if (te >= len) continue;
-                const int bl = s_bl[te];
-                const long long x = (long long)(x0 + te);
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q < nth && bl >= p.th[q]) run[q] = x;
+                for (int q = 0; q < NT; ++q)
+                    if (blv[e] >= th[q]) run[q] = te;
                 Key<W> fkey;
 #pragma unroll
                 for (int w = 0; w < W; ++w) fkey.w[w] = s_keys[(size_t)te * W + w];
 #pragma unroll
                 for (int l = 0; l < 4; ++l) {
                     if (l >= p.nlev) break;
-                    // digit of the unflipped key = flipped bit xor 1
                     if (key_bit<W>(fkey, p.mbit[l]) == 0) {  // original digit 1
-                        const long long sp = pick<8>(run, p.lev_lo[l]), sg = pick<8>(run, p.lev_hi[l]);
+                        const int sp = pick<NT>(run, p.lev_lo[l]), sg = pick<NT>(run, p.lev_hi[l]);
                         disp[e] -= (sp == sg) ? 0 : (sp - sg);
                     }
                 }
             }
         }
-        // backward pass: displacement of the digits that are 0 (move ahead by n1)
         {
-            long long run[8];
+            int run[NT];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) run[q] = cnext[q];
+            for (int q = 0; q < NT; ++q) run[q] = cnext[q];
+#pragma unroll
             for (int e = kP2Items - 1; e >= 0; --e) {
                 const int te = e0 + e;
                 if (te >= len) continue;
-                const int bl = s_bl[te];
-                const long long x = (long long)(x0 + te);
                 Key<W> fkey;
 #pragma unroll
                 for (int w = 0; w < W; ++w) fkey.w[w] = s_keys[(size_t)te * W + w];
@@ -435,20 +448,20 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
                 for (int l = 0; l < 4; ++l) {
                     if (l >= p.nlev) break;
                     if (key_bit<W>(fkey, p.mbit[l]) == 1) {  // original digit 0
-                        const long long sp = pick<8>(run, p.lev_lo[l]), en = pick<8>(run, p.lev_hi[l]);
+                        const int sp = pick<NT>(run, p.lev_lo[l]), en = pick<NT>(run, p.lev_hi[l]);
                         disp[e] += (sp == en) ? 0 : (en - sp);
                     }
                 }
-                const unsigned long long dest = (unsigned long long)(x + disp[e]);
-                if (dest < a) {
-                    store_key<W>(b.sk, dest, fkey);
+                const long long dest = (long long)x0 + te + disp[e];
+                if (dest >= 0 && (unsigned long long)dest < a) {
+                    store_key<W>(b.sk, (unsigned long long)dest, fkey);
                     b.sv[dest] = s_vals[te];
                 } else {
                     atomicOr(&st->status, ST_ORDER);
                 }
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q < nth && bl >= p.th[q]) run[q] = x;
+                for (int q = 0; q < NT; ++q)
+                    if (blv[e] >= th[q]) run[q] = te;
             }
         }
     }
@@ -513,7 +526,7 @@ template <int NT>
 __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned long long ntiles) {
     constexpr int NW = NT / 32;
     constexpr unsigned long long T = kP3Tile + 1;
-    __shared__ double c_l1[NW], c_sq[NW];
+    __shared__ U128 c_l1[NW], c_sq[NW];
     __shared__ unsigned long long c_n, c_a;
     __shared__ unsigned c_status;
     DeviceState* st = b.st;
@@ -542,33 +555,31 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
                 }
             }
         } else {
-            // deterministic fixed-shape tree over the per-tile partials
-            const unsigned long long per = (ntiles + NT - 1) / NT;
-            const unsigned long long lo = threadIdx.x * per;
-            const unsigned long long hi = min(ntiles, lo + per);
-            for (unsigned long long t = lo; t < hi; ++t) {
-                l1 = up_add(l1, __ldcg(b.partials + 2 * t));
-                sq = up_add(sq, __ldcg(b.partials + 2 * t + 1));
+            // exact 128-bit sums of the per-tile fixed-point partials, then
+            // one upward conversion each
+            U128 a1{0ull, 0ull}, a2{0ull, 0ull};
+            for (unsigned long long t = threadIdx.x; t < ntiles; t += NT) {
+                u128_add(a1, U128{__ldcg(b.partials + 4 * t), __ldcg(b.partials + 4 * t + 1)});
+                u128_add(a2, U128{__ldcg(b.partials + 4 * t + 2), __ldcg(b.partials + 4 * t + 3)});
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
-                const double o1 = __shfl_down_sync(0xffffffffu, l1, off);
-                const double o2 = __shfl_down_sync(0xffffffffu, sq, off);
-                l1 = up_add(l1, o1);
-                sq = up_add(sq, o2);
+                u128_add(a1, shfl_down_u128(a1, off));
+                u128_add(a2, shfl_down_u128(a2, off));
             }
             if (lane == 0) {
-                c_l1[warp] = l1;
-                c_sq[warp] = sq;
+                c_l1[warp] = a1;
+                c_sq[warp] = a2;
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                l1 = 0.0;
-                sq = 0.0;
+                U128 t1{0ull, 0ull}, t2{0ull, 0ull};
                 for (int w = 0; w < NW; ++w) {
-                    l1 = up_add(l1, c_l1[w]);
-                    sq = up_add(sq, c_sq[w]);
+                    u128_add(t1, c_l1[w]);
+                    u128_add(t2, c_sq[w]);
                 }
+                l1 = u128_to_double_up(t1, p.fx_unit1);
+                sq = u128_to_double_up(t2, p.fx_unit2);
             }
         }
         if (threadIdx.x == 0) {
@@ -634,7 +645,7 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
     double* s_fv = s_kv + T;
     __shared__ unsigned long long s_tile, s_base_k, s_base_n;
     __shared__ unsigned s_wk[NW], s_wn[NW], s_wr[NW];
-    __shared__ double s_l1[NW], s_sq[NW];
+    __shared__ U128 s_l1[NW], s_sq[NW];
     __shared__ int s_last;
 
     DeviceState* st = b.st;
@@ -715,7 +726,7 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
         double val[MAXI];
         unsigned char cls[MAXI], nx[MAXI];
         unsigned cnt_k = 0, cnt_n = 0, cnt_r = 0;
-        double l1 = 0.0, sq = 0.0;
+        U128 l1{0ull, 0ull}, sq{0ull, 0ull};
         bool bad = false;
 #pragma unroll
         for (int e = 0; e < MAXI; ++e) {
@@ -737,7 +748,9 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
                 ++ik;
                 bool anti, plus;
                 branch_info(p, word_at<W>(key, p.i_word), word_at<W>(key, p.j_word), anti, plus);
-                v = anti ? __dmul_rn(vin, c) : __dadd_rn(vin, 0.0);
+                // commuting: the reference sums (v) + (+0), which is v for v != 0
+                // and +0 for a zero (dropped below either way)
+                v = anti ? __dmul_rn(vin, c) : vin;
                 // the partner (if any) is the next merged element: sum it here
                 if (jf < nf && key_eq<W>(fkey(jf), key)) v = __dadd_rn(v, s_fv[jf]);
             } else {
@@ -749,13 +762,17 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
                 if (ik > 0 && key_eq<W>(kkey(ik - 1), key)) continue;
             }
             if (!is_finite(v)) bad = true;
-            if (v == 0.0) continue;  // exact cancellation: dropped, no ledger entry
+            if (is_zero(v)) continue;  // exact cancellation: dropped, no ledger entry
             val[e] = v;
-            if (!key_is_zero<W>(key) && fabs(v) <= p.threshold) {
+            if (!key_is_zero<W>(key) && abs_bits(v) <= p.threshold_bits) {
                 cls[e] = 2;
                 ++cnt_r;
-                l1 = up_add(l1, fabs(v));
-                sq = up_add(sq, up_mul(v, v));
+                if (!p.exact_ledger) {
+                    U128 x1, x2;
+                    fixed_terms(v, p.fx_unit1, p.fx_unit2, x1, x2);
+                    u128_add(l1, x1);
+                    u128_add(sq, x2);
+                }
             } else {
                 cls[e] = 1;
                 ++cnt_k;
@@ -785,14 +802,14 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
                 sr_ += tr;
             }
         }
-        // ledger partials: deterministic tree within the warp, then across warps
-        double wl1 = l1, wsq = sq;
+        // ledger partials: exact 128-bit sums within the warp, then across warps
+        U128 wl1 = l1, wsq = sq;
+        if (!p.exact_ledger) {
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const double o1 = __shfl_down_sync(0xffffffffu, wl1, off);
-            const double o2 = __shfl_down_sync(0xffffffffu, wsq, off);
-            wl1 = up_add(wl1, o1);
-            wsq = up_add(wsq, o2);
+            for (int off = 16; off > 0; off >>= 1) {
+                u128_add(wl1, shfl_down_u128(wl1, off));
+                u128_add(wsq, shfl_down_u128(wsq, off));
+            }
         }
         if (lane == 31) {
             s_wk[warp] = sk_;
@@ -823,13 +840,17 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
                 unpack2(base, bk, bn);
                 s_base_k = bk;
                 s_base_n = bn;
-                double t1 = 0.0, t2 = 0.0;
-                for (int w = 0; w < NW; ++w) {
-                    t1 = up_add(t1, s_l1[w]);
-                    t2 = up_add(t2, s_sq[w]);
+                if (!p.exact_ledger) {
+                    U128 t1{0ull, 0ull}, t2{0ull, 0ull};
+                    for (int w = 0; w < NW; ++w) {
+                        u128_add(t1, s_l1[w]);
+                        u128_add(t2, s_sq[w]);
+                    }
+                    b.partials[4 * tile] = t1.lo;
+                    b.partials[4 * tile + 1] = t1.hi;
+                    b.partials[4 * tile + 2] = t2.lo;
+                    b.partials[4 * tile + 3] = t2.hi;
                 }
-                b.partials[2 * tile] = t1;
-                b.partials[2 * tile + 1] = t2;
                 b.rem_count[tile] = tr_tot;
                 if (tr_tot) atomicAdd(&st->removed, (unsigned long long)tr_tot);
                 if (tile == ntiles - 1) {
@@ -861,14 +882,15 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
                     if (on < b.cap) {
                         const double y = __dmul_rn(val[e], sn);
                         store_key<W>(b.fk, on, key_xor<W>(key, MN));
-                        b.fv[on] = nx[e] == 1 ? y : -y;
+                        reinterpret_cast<unsigned long long*>(b.fv)[on] =
+                            dbits(y) ^ (nx[e] == 1 ? 0ull : kSignBit);
                     } else {
                         atomicOr(&st->status, ST_CAPACITY);
                     }
                     ++on;
                 }
             } else {
-                if (p.exact_ledger) b.rem[tile * (unsigned long long)T + orr] = fabs(val[e]);
+                if (p.exact_ledger) b.rem[tile * (unsigned long long)T + orr] = abs_of(val[e]);
                 ++orr;
             }
         }
