@@ -229,7 +229,7 @@ def prepare_state(eng, cfg, target_terms, max_setup_steps, opts):
     led = GbLedger()
     steps = 0
     while len(m) < target_terms and steps < max_setup_steps:
-        chunk = 1 if len(m) > target_terms / 4 else 4
+        chunk = 1 if len(m) > target_terms * 0.9 else 5
         st, _, led, msg = m.evolve(terms, cfg["dt"], chunk, opts, led, record_fid=False)
         if st:
             raise RuntimeError(f"set-up evolve failed: {msg}")
@@ -404,9 +404,10 @@ def run_reference(args, dist):
     from ddevol_gb300.engine import Engine, options
     cfg = CONFIGS[args.config]
     words = (cfg["n"] + 31) // 32
-    # set-up only: the window-start state comes from the device engine (untimed)
+    # set-up only: the window-start state comes from the device engine (untimed);
+    # keys and values do not depend on the ledger mode, so the fast ledger is used
     eng = Engine(dist.local_rank)
-    opts = options(cfg["threshold"], exact_ledger=True)
+    opts = options(cfg["threshold"], exact_ledger=False)
     m, terms, _, setup_steps = prepare_state(eng, cfg, args.target_terms, args.max_setup_steps,
                                              opts)
     k, v = m.download()
@@ -447,7 +448,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="ring64")
-    ap.add_argument("--target-terms", type=float, default=4e6)
+    ap.add_argument("--target-terms", type=float, default=1e5,
+                    help="set-up evolves until the map holds this many terms")
     ap.add_argument("--max-setup-steps", type=int, default=400)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
