@@ -349,3 +349,158 @@ extern "C" tpgp_cuda_status tpgp_cuda_branches(tpgp_cuda_context* ctx, const uin
         result = cuda_failure(code, "CUDA previous-device restoration", error, cap);
     return result;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of tpgp_cuda_branches.
+//
+// Some callers cannot call cudaMalloc: code running inside a host allocator
+// or a signal-safe/real-time section, plugins whose host application owns
+// all device memory, or processes whose device memory is fully reserved by
+// another runtime.  For them the device staging buffers of the branch kernel
+// (input keys/values, output keys/values/radii, failure flag) live in one
+// file-scope array that the library's module brings with it; the call itself
+// allocates nothing.
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;  // 16 MiB per device
+static __device__ __align__(256) unsigned char g_branch_scratch[kStaticScratchBytes];
+
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_lock;                                 // serializes every call
+void* g_static_address[kMaxStaticDevices] = {nullptr};    // device address, per device
+
+}  // namespace
+
+extern "C" tpgp_cuda_status tpgp_cuda_branches_static(
+    int device_index, const uint64_t* keys, const double* values, size_t count, size_t words,
+    size_t spins, size_t i, size_t j, unsigned qi, unsigned qj, double c, double s, double rc,
+    double rs, int enclose, uint64_t* out_keys, double* out_values, double* out_radii,
+    char* error, size_t cap) {
+    set_message(error, cap, "");
+    // the same argument checks, in the same order, as tpgp_cuda_branches
+    if (device_index < 0 || device_index >= kMaxStaticDevices || spins < 2 ||
+        words != spins / 32 + (spins % 32 != 0) || i >= spins || j >= spins || i == j ||
+        qi > 3 || qj > 3 || !std::isfinite(c) || !std::isfinite(s) || !std::isfinite(rc) ||
+        !std::isfinite(rs) || rc < 0 || rs < 0 || (enclose != 0 && enclose != 1)) {
+        set_message(error, cap,
+                    "Invalid CUDA branch device, dimensions, sites, generator, or trigonometric enclosure.");
+        return TPGP_CUDA_EINVAL;
+    }
+    if (!count) return TPGP_CUDA_OK;
+    size_t key_bytes, value_bytes, out_key_bytes, out_value_bytes, total, t;
+    if (!keys || !values || !out_keys || !out_values || !out_radii || !mul_ok(count, words, &t) ||
+        !mul_ok(t, sizeof(uint64_t), &key_bytes) || !mul_ok(count, sizeof(double), &value_bytes) ||
+        !mul_ok(key_bytes, 2, &out_key_bytes) || !mul_ok(value_bytes, 2, &out_value_bytes) ||
+        !mul_ok(key_bytes, 3, &total) || !mul_ok(value_bytes, 5, &t) || !add_ok(total, t, &total) ||
+        !add_ok(total, 128, &total)) {
+        set_message(error, cap, "Null CUDA array or packed-branch size overflow.");
+        return TPGP_CUDA_EINVAL;
+    }
+    if (total > kStaticScratchBytes) {
+        if (error && cap)
+            std::snprintf(error, cap,
+                          "Batch needs %zu bytes of staging; the allocation-free entry point holds "
+                          "at most %zu bytes ((24*n_words + 40) bytes per term). Split the batch.",
+                          total, kStaticScratchBytes);
+        return TPGP_CUDA_EINVAL;
+    }
+    const void* arrays[] = {keys, values, out_keys, out_values, out_radii};
+    const size_t lengths[] = {key_bytes, value_bytes, out_key_bytes, out_value_bytes,
+                              out_value_bytes};
+    for (int x = 0; x < 5; ++x)
+        for (int y = x + 1; y < 5; ++y)
+            if (ranges_overlap(arrays[x], lengths[x], arrays[y], lengths[y])) {
+                set_message(error, cap, "CUDA input/output arrays must be disjoint.");
+                return TPGP_CUDA_EINVAL;
+            }
+    std::lock_guard<std::mutex> guard(g_static_lock);
+    tpgp_cuda_status result = TPGP_CUDA_OK;
+    int previous = 0, count_dev = 0;
+    cudaError_t code = cudaGetDeviceCount(&count_dev);
+    if (code != cudaSuccess) return cuda_failure(code, "CUDA device discovery", error, cap);
+    if (device_index >= count_dev) {
+        set_message(error, cap, "Requested CUDA device index is unavailable.");
+        return TPGP_CUDA_EINVAL;
+    }
+    if ((code = cudaGetDevice(&previous)) != cudaSuccess)
+        return cuda_failure(code, "CUDA current-device query", error, cap);
+    if ((code = cudaSetDevice(device_index)) != cudaSuccess)
+        return cuda_failure(code, "CUDA device selection", error, cap);
+    // set-up, once per device, with that device current: the host-side name
+    // of the array is not a device address, so ask the runtime for it
+    if (!g_static_address[device_index]) {
+        void* ptr = nullptr;
+        code = cudaGetSymbolAddress(&ptr, g_branch_scratch);
+        if (code != cudaSuccess) {
+            result = cuda_failure(code, "CUDA static scratch address", error, cap);
+            cudaSetDevice(previous);
+            return result;
+        }
+        g_static_address[device_index] = ptr;
+    }
+    unsigned char* base = static_cast<unsigned char*>(g_static_address[device_index]);
+    auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
+    size_t off = 0;
+    uint64_t* d_out_keys = reinterpret_cast<uint64_t*>(base + off);
+    off = align16(off + out_key_bytes);
+    double* d_out_values = reinterpret_cast<double*>(base + off);
+    off = align16(off + out_value_bytes);
+    double* d_out_radii = reinterpret_cast<double*>(base + off);
+    off = align16(off + out_value_bytes);
+    uint64_t* d_keys = reinterpret_cast<uint64_t*>(base + off);
+    off = align16(off + key_bytes);
+    double* d_values = reinterpret_cast<double*>(base + off);
+    off = align16(off + value_bytes);
+    unsigned* d_failure = reinterpret_cast<unsigned*>(base + off);
+    unsigned failure = 0;
+#define STEP(call, what)                                                      \
+    do {                                                                      \
+        if (result == TPGP_CUDA_OK) {                                         \
+            code = (call);                                                    \
+            if (code != cudaSuccess) result = cuda_failure(code, what, error, cap); \
+        }                                                                     \
+    } while (0)
+    STEP(cudaMemcpy(d_keys, keys, key_bytes, cudaMemcpyHostToDevice), "CUDA input-key transfer");
+    STEP(cudaMemcpy(d_values, values, value_bytes, cudaMemcpyHostToDevice),
+         "CUDA input-coefficient transfer");
+    // the array keeps the previous call's contents: the failure flag must start at zero
+    STEP(cudaMemset(d_failure, 0, sizeof(unsigned)), "CUDA status reset");
+    if (result == TPGP_CUDA_OK) {
+        int sms = 1;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_index);
+        const size_t want = (count + 255) / 256, cap_blocks = (size_t)(sms > 0 ? sms : 1) * 16;
+        const unsigned blocks = (unsigned)(want < cap_blocks ? want : cap_blocks);
+        if (words == 1)
+            k_branch<1><<<blocks, 256>>>(d_keys, d_values, count, words, spins, i, j, qi, qj, c,
+                                         s, rc, rs, enclose, d_out_keys, d_out_values,
+                                         d_out_radii, d_failure);
+        else if (words == 2)
+            k_branch<2><<<blocks, 256>>>(d_keys, d_values, count, words, spins, i, j, qi, qj, c,
+                                         s, rc, rs, enclose, d_out_keys, d_out_values,
+                                         d_out_radii, d_failure);
+        else
+            k_branch<0><<<blocks, 256>>>(d_keys, d_values, count, words, spins, i, j, qi, qj, c,
+                                         s, rc, rs, enclose, d_out_keys, d_out_values,
+                                         d_out_radii, d_failure);
+        STEP(cudaGetLastError(), "CUDA branch-kernel launch");
+    }
+    STEP(cudaMemcpy(&failure, d_failure, sizeof(unsigned), cudaMemcpyDeviceToHost),
+         "CUDA branch-kernel execution");
+    if (result == TPGP_CUDA_OK && failure) {
+        result = (failure & 1u) ? TPGP_CUDA_EINVAL : TPGP_CUDA_ENUMERIC;
+        set_message(error, cap,
+                    (failure & 1u) ? "CUDA input keys contain nonzero padding bits."
+                                   : "CUDA branch arithmetic or coefficients are nonfinite.");
+    }
+    STEP(cudaMemcpy(out_keys, d_out_keys, out_key_bytes, cudaMemcpyDeviceToHost),
+         "CUDA output-key transfer");
+    STEP(cudaMemcpy(out_values, d_out_values, out_value_bytes, cudaMemcpyDeviceToHost),
+         "CUDA output-coefficient transfer");
+    STEP(cudaMemcpy(out_radii, d_out_radii, out_value_bytes, cudaMemcpyDeviceToHost),
+         "CUDA output-radius transfer");
+#undef STEP
+    code = cudaSetDevice(previous);
+    if (result == TPGP_CUDA_OK && code != cudaSuccess)
+        result = cuda_failure(code, "CUDA previous-device restoration", error, cap);
+    return result;
+}

@@ -58,6 +58,10 @@ def _bind(lib):
     lib.tpgp_cuda_branches.argtypes = [
         C.c_void_p, u64p, f64p, sz, sz, sz, sz, sz, C.c_uint, C.c_uint, C.c_double, C.c_double,
         C.c_double, C.c_double, C.c_int, u64p, f64p, f64p, charp, sz]
+    lib.tpgp_cuda_branches_static.restype = C.c_int
+    lib.tpgp_cuda_branches_static.argtypes = [
+        C.c_int, u64p, f64p, sz, sz, sz, sz, sz, C.c_uint, C.c_uint, C.c_double, C.c_double,
+        C.c_double, C.c_double, C.c_int, u64p, f64p, f64p, charp, sz]
     # device-resident ABI
     lib.tpgp_gb_compiled.restype = C.c_int
     lib.tpgp_gb_default_options.restype = GbOptions
