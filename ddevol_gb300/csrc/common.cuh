@@ -38,34 +38,34 @@ struct Key {
     uint64_t w[W];
 };
 
+// Loads of kernel data use ld.global.cg (L2, not the L1 or read-only
+// caches): the persistent step kernel reads, after a grid barrier, buffers
+// that other SMs wrote earlier in the same launch, where an L1 or
+// non-coherent cached copy could be stale.
 template <int W>
-__device__ __forceinline__ Key<W> load_key(const uint64_t* __restrict__ keys, size_t k) {
+__device__ __forceinline__ Key<W> load_key(const uint64_t* keys, size_t k) {
     Key<W> r;
     if constexpr (W == 2) {
-        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(keys) + k);
+        const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(keys) + k);
         r.w[0] = v.x;
         r.w[1] = v.y;
     } else if constexpr (W == 4) {
-        const ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(keys) + 2 * k);
-        const ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(keys) + 2 * k + 1);
+        const ulonglong2 a = __ldcg(reinterpret_cast<const ulonglong2*>(keys) + 2 * k);
+        const ulonglong2 b = __ldcg(reinterpret_cast<const ulonglong2*>(keys) + 2 * k + 1);
         r.w[0] = a.x;
         r.w[1] = a.y;
         r.w[2] = b.x;
         r.w[3] = b.y;
     } else {
 #pragma unroll
-        for (int w = 0; w < W; ++w) r.w[w] = __ldg(keys + k * W + w);
+        for (int w = 0; w < W; ++w) r.w[w] = __ldcg(keys + k * W + w);
     }
     return r;
 }
 
-// Plain (coherent) load for buffers written earlier in the same kernel.
 template <int W>
 __device__ __forceinline__ Key<W> load_key_coherent(const uint64_t* keys, size_t k) {
-    Key<W> r;
-#pragma unroll
-    for (int w = 0; w < W; ++w) r.w[w] = keys[k * W + w];
-    return r;
+    return load_key<W>(keys, k);
 }
 
 template <int W>
@@ -326,6 +326,8 @@ struct DeviceState {
     unsigned long long a_next;   // anticommuting terms of the next rotation (set by k_merge)
     unsigned int status;         // sticky ST_* bits
     unsigned int p1_counter, p3_counter, merge_done;
+    unsigned int bar_count, bar_gen;  // grid barrier of the persistent kernel
+    unsigned int stop;                // set by the committing CTA when the rotation failed
     unsigned long long p1_tiles, p3_tiles;  // tiles used (cleared by the commit kernel)
     unsigned long long rotations_done;      // rotations committed in the current call
     unsigned long long terms_in;            // input terms of the committed rotations

@@ -122,13 +122,13 @@ __device__ __forceinline__ Key<W> mask_key(const RotParams& p) {
 
 // ======================================================================= P1
 template <int W>
-__global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
+__device__ void phase_classify(const RotParams& p, const Buffers& b) {
     constexpr int NW = kP1Block / 32;
     __shared__ unsigned s_counts[kP1Items * NW];
     __shared__ unsigned long long s_tile, s_base;
     DeviceState* st = b.st;
-    if (st->status) return;
-    const unsigned long long n = st->n;
+    if (__ldcg(&st->status)) return;
+    const unsigned long long n = __ldcg(&st->n);
     const unsigned long long ntiles = (n + kP1Tile - 1) / kP1Tile;
     if (blockIdx.x >= ntiles) return;  // never needed: fewer tiles than CTAs
     const Key<W> M = mask_key<W>(p);
@@ -149,10 +149,10 @@ __global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
             anti[e] = false;
             plus[e] = false;
             if (k < n) {
-                const uint64_t wi = __ldg(b.in_keys + k * W + p.i_word);
-                const uint64_t wj = __ldg(b.in_keys + k * W + p.j_word);
+                const uint64_t wi = __ldcg(b.in_keys + k * W + p.i_word);
+                const uint64_t wj = __ldcg(b.in_keys + k * W + p.j_word);
                 branch_info(p, wi, wj, anti[e], plus[e]);
-                const double v = __ldg(b.in_vals + k);
+                const double v = __ldcg(b.in_vals + k);
                 // the reference rejects any nonfinite raw child (tpgp_rev.c:682-688)
                 if (!is_finite(v)) bad = true;
             }
@@ -201,12 +201,17 @@ __global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
                 continue;
             }
             const Key<W> key = load_key<W>(b.in_keys, k);
-            const double v = __ldg(b.in_vals + k);
+            const double v = __ldcg(b.in_vals + k);
             const double y = __dmul_rn(v, p.s);
             store_key<W>(b.fk, x, key_xor<W>(key, M));
             reinterpret_cast<unsigned long long*>(b.fv)[x] = dbits(y) ^ (plus[e] ? 0ull : kSignBit);
         }
     }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
+    phase_classify<W>(p, b);
 }
 
 // ======================================================================= P2
@@ -274,8 +279,7 @@ __device__ unsigned long long run_edge(const uint64_t* fk, const Key<W>& M,
 // each site carries one mask bit, 6 otherwise).  Positions inside the kernel
 // are 32-bit and relative to the tile start (a map holds < 2^30 terms).
 template <int W, int NT>
-__global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* smem_raw) {
     uint64_t* s_keys = reinterpret_cast<uint64_t*>(smem_raw);                 // [tile][W]
     double* s_vals = reinterpret_cast<double*>(s_keys + (size_t)kP2Tile * W);  // [tile]
     short* s_bl = reinterpret_cast<short*>(s_vals + kP2Tile);                 // [tile]
@@ -284,8 +288,8 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
     constexpr int kNone = INT_MIN, kEnd = INT_MAX;
 
     DeviceState* st = b.st;
-    if (st->status) return;
-    const unsigned long long a = st->a;
+    if (__ldcg(&st->status)) return;
+    const unsigned long long a = __ldcg(&st->a);
     if (a == 0 || p.nlev == 0) return;
     const unsigned long long ntiles = (a + kP2Tile - 1) / kP2Tile;
     const Key<W> M = mask_key<W>(p);
@@ -304,7 +308,7 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
             const Key<W> k = load_key<W>(b.fk, x0 + e);
 #pragma unroll
             for (int w = 0; w < W; ++w) s_keys[(size_t)e * W + w] = k.w[w];
-            s_vals[e] = __ldg(b.fv + x0 + e);
+            s_vals[e] = __ldcg(b.fv + x0 + e);
         }
         // run edges outside the tile for every threshold (galloping searches),
         // as offsets from x0
@@ -467,15 +471,21 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
     }
 }
 
+template <int W, int NT>
+__global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    phase_flip<W, NT>(p, b, smem_raw);
+}
+
 // ====================================================================== P3a
 // One warp per tile boundary: a 32-ary search along the merge-path diagonal
 // (each round the 32 lanes probe 32 evenly spaced positions in parallel), so
 // a split costs ~log_32(n) dependent memory round trips instead of log_2(n).
 template <int W>
-__global__ void k_partition(RotParams p, Buffers b) {
+__device__ void phase_partition(const RotParams& p, const Buffers& b) {
     DeviceState* st = b.st;
-    if (st->status) return;
-    const unsigned long long n = st->n, a = st->a, L = n + a;
+    if (__ldcg(&st->status)) return;
+    const unsigned long long n = __ldcg(&st->n), a = __ldcg(&st->a), L = n + a;
     const unsigned long long ntiles = (L + kP3Tile - 1) / kP3Tile;
     const unsigned lane = lane_id();
     const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
@@ -509,6 +519,11 @@ __global__ void k_partition(RotParams p, Buffers b) {
             b.splits[2 * t + 1] = j;
         }
     }
+}
+
+template <int W>
+__global__ void k_partition(RotParams p, Buffers b) {
+    phase_partition<W>(p, b);
 }
 
 // ====================================================================== P3b
@@ -587,7 +602,15 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
             const unsigned long long removed = __ldcg(&st->removed);
             unsigned fail = 0;
             if (p.max_terms && n_out > p.max_terms) fail = ST_CAP;
-            Ledger next = st->ledger;
+            Ledger next;
+            next.dropped_l1 = __ldcg(&st->ledger.dropped_l1);
+            next.dropped_l2 = __ldcg(&st->ledger.dropped_l2);
+            next.dropped_l2_squared = __ldcg(&st->ledger.dropped_l2_squared);
+            next.arithmetic_l2 = __ldcg(&st->ledger.arithmetic_l2);
+            next.rotations = __ldcg(&st->ledger.rotations);
+            next.removal_events = __ldcg(&st->ledger.removal_events);
+            next.peak_terms = __ldcg(&st->ledger.peak_terms);
+            next.arithmetic_enclosed = __ldcg(&st->ledger.arithmetic_enclosed);
             if (!fail) {
                 const double l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
                 next.dropped_l1 = up_add(next.dropped_l1, l1);
@@ -607,12 +630,12 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
                 st->ledger = next;
                 st->n = n_out;
                 st->a = p.has_next ? __ldcg(&st->a_next) : 0;
-                st->rotations_done += 1;
-                st->terms_in += n;
+                st->rotations_done = __ldcg(&st->rotations_done) + 1;
+                st->terms_in = __ldcg(&st->terms_in) + n;
             }
         }
     } else if (!status && threadIdx.x == 0) {
-        st->rotations_done += 1;  // empty map: a no-op rotation, no ledger change
+        st->rotations_done = __ldcg(&st->rotations_done) + 1;  // empty map: no-op, no ledger change
         st->a = 0;
     }
     __syncthreads();
@@ -630,15 +653,20 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
         st->n_out = 0;
         st->removed = 0;
         st->a_next = 0;
+        // read by every CTA of the persistent kernel after the next barrier
+        st->stop = __ldcg(&st->status) != 0 ? 1u : 0u;
     }
     (void)c_a;
 }
 
+// every_cta: all CTAs of the grid run this phase (persistent kernel), so all
+// of them take part in electing the committing CTA; otherwise only the CTAs
+// that can find a tile take part.
 template <int W>
-__global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
+__device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char* smem_raw,
+                            bool every_cta) {
     constexpr int T = kP3Tile + 1;  // one extra slot for a pair moved across the boundary
     constexpr int NW = kP3Block / 32;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* s_kk = reinterpret_cast<uint64_t*>(smem_raw);       // cos-list keys [T][W]
     uint64_t* s_fk = s_kk + (size_t)T * W;                        // sorted flipped keys
     double* s_kv = reinterpret_cast<double*>(s_fk + (size_t)T * W);
@@ -649,11 +677,14 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
     __shared__ int s_last;
 
     DeviceState* st = b.st;
-    if (st->status) return;
-    const unsigned long long n = st->n, a = st->a, L = n + a;
-    const unsigned long long ntiles = (L + kP3Tile - 1) / kP3Tile;
+    // in the persistent kernel every CTA must reach the commit election even
+    // after a failure, so a set status only skips the tile work
+    const bool failed = *reinterpret_cast<volatile unsigned*>(&st->status) != 0;
+    if (failed && !every_cta) return;
+    const unsigned long long n = __ldcg(&st->n), a = __ldcg(&st->a), L = n + a;
+    const unsigned long long ntiles = failed ? 0 : (L + kP3Tile - 1) / kP3Tile;
     const unsigned long long participants =
-        max(1ull, min((unsigned long long)gridDim.x, ntiles));
+        every_cta ? (unsigned long long)gridDim.x : max(1ull, min((unsigned long long)gridDim.x, ntiles));
     if (blockIdx.x >= participants) return;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const double c = p.c;
@@ -666,8 +697,8 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
         __syncthreads();
         const unsigned long long tile = s_tile;
         if (tile >= ntiles) break;
-        const unsigned long long i0 = b.splits[2 * tile], j0 = b.splits[2 * tile + 1];
-        const unsigned long long i1 = b.splits[2 * tile + 2], j1 = b.splits[2 * tile + 3];
+        const unsigned long long i0 = __ldcg(b.splits + 2 * tile), j0 = __ldcg(b.splits + 2 * tile + 1);
+        const unsigned long long i1 = __ldcg(b.splits + 2 * tile + 2), j1 = __ldcg(b.splits + 2 * tile + 3);
         int nk = (int)(i1 - i0), nf = (int)(j1 - j0);
         // the split points guarantee 0 <= nk, nf and nk + nf <= T; a tile that
         // breaks this is flagged and processed as empty (it still publishes
@@ -682,13 +713,13 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
             const Key<W> k = load_key<W>(b.in_keys, i0 + e);
 #pragma unroll
             for (int w = 0; w < W; ++w) s_kk[(size_t)e * W + w] = k.w[w];
-            s_kv[e] = __ldg(b.in_vals + i0 + e);
+            s_kv[e] = __ldcg(b.in_vals + i0 + e);
         }
         for (int e = threadIdx.x; e < nf; e += kP3Block) {
             const Key<W> k = load_key<W>(b.sk, j0 + e);
 #pragma unroll
             for (int w = 0; w < W; ++w) s_fk[(size_t)e * W + w] = k.w[w];
-            s_fv[e] = b.sv[j0 + e];
+            s_fv[e] = __ldcg(b.sv + j0 + e);
         }
         __syncthreads();
         auto kkey = [&](int e) {
@@ -905,6 +936,92 @@ __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
     if (!s_last) return;
     __threadfence();
     commit_rotation<kP3Block>(p, b, ntiles);
+}
+
+template <int W>
+__global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    phase_merge<W>(p, b, smem_raw, false);
+}
+
+// ============================================================== persistent
+// One cooperative launch runs a whole list of rotations: the same phases as
+// the per-kernel path, separated by grid barriers instead of kernel
+// boundaries.  All CTAs are co-resident (cooperative launch), and every
+// barrier wait is bounded: a wait that gives up sets ST_TIMEOUT and the CTA
+// leaves the kernel, so no launch can spin forever.
+constexpr unsigned kBarrierPolls = 1u << 24;
+
+// false if the wait gave up
+__device__ inline bool grid_barrier(DeviceState* st) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &st->bar_gen;
+        const unsigned g = *gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&st->bar_count, 1u);
+        int ok = 1;
+        if (arrived == gridDim.x - 1) {
+            atomicExch(&st->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&st->bar_gen, 1u);
+        } else {
+            unsigned polls = 0;
+            while (*gen == g) {
+                if (++polls > kBarrierPolls) {
+                    atomicOr(&st->status, ST_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+struct StepArgs {
+    const RotParams* ps;     // rotation list in device memory
+    unsigned rotations;
+    uint64_t* keys[3];       // the three map buffers
+    double* vals[3];
+    int x, y, z;             // step input, then the two ping-pong buffers
+    Buffers scratch;         // fk..st, cap (in/out filled per rotation)
+};
+
+template <int W>
+__global__ void __launch_bounds__(kP3Block, 2) k_step(StepArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DeviceState* st = a.scratch.st;
+    for (unsigned r = 0; r < a.rotations; ++r) {
+        const RotParams& p = a.ps[r];
+        const int in = r == 0 ? a.x : ((r - 1) % 2 == 0 ? a.y : a.z);
+        const int out = r % 2 == 0 ? a.y : a.z;
+        Buffers b = a.scratch;
+        b.in_keys = a.keys[in];
+        b.in_vals = a.vals[in];
+        b.out_keys = a.keys[out];
+        b.out_vals = a.vals[out];
+        if (r == 0) {
+            phase_classify<W>(p, b);
+            if (!grid_barrier(st)) return;
+        }
+        // phases skip their work once the status is set; the merge phase
+        // still elects a committing CTA, which raises st->stop
+        if (p.nth <= 4) phase_flip<W, 4>(p, b, smem_raw);
+        else phase_flip<W, 6>(p, b, smem_raw);
+        if (!grid_barrier(st)) return;
+        phase_partition<W>(p, b);
+        if (!grid_barrier(st)) return;
+        phase_merge<W>(p, b, smem_raw, true);
+        if (!grid_barrier(st)) return;
+        // written only by the committing CTA before this barrier: uniform
+        if (*reinterpret_cast<volatile unsigned*>(&st->stop)) return;
+    }
 }
 
 }  // namespace tg
