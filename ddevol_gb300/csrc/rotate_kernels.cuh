@@ -104,6 +104,13 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+// The CTAs that run a phase for one map: the whole grid (per-kernel path and
+// persistent kernel) or the CTAs of one thread-block cluster (batched maps).
+struct Grid {
+    unsigned cta, ncta;
+};
+__device__ __forceinline__ Grid whole_grid() { return Grid{blockIdx.x, gridDim.x}; }
+
 // Per-term branch data: anticommutation, phase sign.
 __device__ __forceinline__ void branch_info(const RotParams& p, uint64_t wi, uint64_t wj,
                                             bool& anti, bool& plus) {
@@ -122,7 +129,7 @@ __device__ __forceinline__ Key<W> mask_key(const RotParams& p) {
 
 // ======================================================================= P1
 template <int W>
-__device__ void phase_classify(const RotParams& p, const Buffers& b) {
+__device__ void phase_classify(const RotParams& p, const Buffers& b, Grid g) {
     constexpr int NW = kP1Block / 32;
     __shared__ unsigned s_counts[kP1Items * NW];
     __shared__ unsigned long long s_tile, s_base;
@@ -130,7 +137,7 @@ __device__ void phase_classify(const RotParams& p, const Buffers& b) {
     if (__ldcg(&st->status)) return;
     const unsigned long long n = __ldcg(&st->n);
     const unsigned long long ntiles = (n + kP1Tile - 1) / kP1Tile;
-    if (blockIdx.x >= ntiles) return;  // never needed: fewer tiles than CTAs
+    if (g.cta >= ntiles) return;  // never needed: fewer tiles than CTAs
     const Key<W> M = mask_key<W>(p);
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     for (;;) {
@@ -211,7 +218,7 @@ __device__ void phase_classify(const RotParams& p, const Buffers& b) {
 
 template <int W>
 __global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
-    phase_classify<W>(p, b);
+    phase_classify<W>(p, b, whole_grid());
 }
 
 // ======================================================================= P2
@@ -279,7 +286,7 @@ __device__ unsigned long long run_edge(const uint64_t* fk, const Key<W>& M,
 // each site carries one mask bit, 6 otherwise).  Positions inside the kernel
 // are 32-bit and relative to the tile start (a map holds < 2^30 terms).
 template <int W, int NT>
-__device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* smem_raw) {
+__device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* smem_raw, Grid g) {
     uint64_t* s_keys = reinterpret_cast<uint64_t*>(smem_raw);                 // [tile][W]
     double* s_vals = reinterpret_cast<double*>(s_keys + (size_t)kP2Tile * W);  // [tile]
     short* s_bl = reinterpret_cast<short*>(s_vals + kP2Tile);                 // [tile]
@@ -299,7 +306,7 @@ __device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* 
 #pragma unroll
     for (int q = 0; q < NT; ++q) th[q] = q < nth ? p.th[q] : 0x7fffffff;  // unused: never reached
 
-    for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (unsigned long long tile = g.cta; tile < ntiles; tile += g.ncta) {
         const unsigned long long x0 = tile * kP2Tile;
         const int len = (int)((a - x0) < (unsigned long long)kP2Tile ? (a - x0) : (unsigned long long)kP2Tile);
         const unsigned long long x1 = x0 + len;
@@ -474,7 +481,7 @@ __device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* 
 template <int W, int NT>
 __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    phase_flip<W, NT>(p, b, smem_raw);
+    phase_flip<W, NT>(p, b, smem_raw, whole_grid());
 }
 
 // ====================================================================== P3a
@@ -482,14 +489,14 @@ __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) 
 // (each round the 32 lanes probe 32 evenly spaced positions in parallel), so
 // a split costs ~log_32(n) dependent memory round trips instead of log_2(n).
 template <int W>
-__device__ void phase_partition(const RotParams& p, const Buffers& b) {
+__device__ void phase_partition(const RotParams& p, const Buffers& b, Grid g) {
     DeviceState* st = b.st;
     if (__ldcg(&st->status)) return;
     const unsigned long long n = __ldcg(&st->n), a = __ldcg(&st->a), L = n + a;
     const unsigned long long ntiles = (L + kP3Tile - 1) / kP3Tile;
     const unsigned lane = lane_id();
-    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
-    for (unsigned long long t = (unsigned long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const unsigned long long warps = (unsigned long long)g.ncta * (blockDim.x / 32);
+    for (unsigned long long t = (unsigned long long)g.cta * (blockDim.x / 32) + (threadIdx.x >> 5);
          t <= ntiles; t += warps) {
         const unsigned long long d = min(t * (unsigned long long)kP3Tile, L);
         // smallest i in [lo, hi] with K[i] merged after S[d-i-1] (ties: cos list first)
@@ -523,7 +530,7 @@ __device__ void phase_partition(const RotParams& p, const Buffers& b) {
 
 template <int W>
 __global__ void k_partition(RotParams p, Buffers b) {
-    phase_partition<W>(p, b);
+    phase_partition<W>(p, b, whole_grid());
 }
 
 // ====================================================================== P3b
@@ -664,7 +671,7 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
 // that can find a tile take part.
 template <int W>
 __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char* smem_raw,
-                            bool every_cta) {
+                            bool every_cta, Grid g) {
     constexpr int T = kP3Tile + 1;  // one extra slot for a pair moved across the boundary
     constexpr int NW = kP3Block / 32;
     uint64_t* s_kk = reinterpret_cast<uint64_t*>(smem_raw);       // cos-list keys [T][W]
@@ -684,8 +691,8 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
     const unsigned long long n = __ldcg(&st->n), a = __ldcg(&st->a), L = n + a;
     const unsigned long long ntiles = failed ? 0 : (L + kP3Tile - 1) / kP3Tile;
     const unsigned long long participants =
-        every_cta ? (unsigned long long)gridDim.x : max(1ull, min((unsigned long long)gridDim.x, ntiles));
-    if (blockIdx.x >= participants) return;
+        every_cta ? (unsigned long long)g.ncta : max(1ull, min((unsigned long long)g.ncta, ntiles));
+    if (g.cta >= participants) return;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const double c = p.c;
     Key<W> MN;
@@ -941,7 +948,7 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
 template <int W>
 __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    phase_merge<W>(p, b, smem_raw, false);
+    phase_merge<W>(p, b, smem_raw, false, whole_grid());
 }
 
 // ============================================================== persistent
@@ -1006,22 +1013,121 @@ __global__ void __launch_bounds__(kP3Block, 2) k_step(StepArgs a) {
         b.in_vals = a.vals[in];
         b.out_keys = a.keys[out];
         b.out_vals = a.vals[out];
+        const Grid g = whole_grid();
         if (r == 0) {
-            phase_classify<W>(p, b);
+            phase_classify<W>(p, b, g);
             if (!grid_barrier(st)) return;
         }
         // phases skip their work once the status is set; the merge phase
         // still elects a committing CTA, which raises st->stop
-        if (p.nth <= 4) phase_flip<W, 4>(p, b, smem_raw);
-        else phase_flip<W, 6>(p, b, smem_raw);
+        if (p.nth <= 4) phase_flip<W, 4>(p, b, smem_raw, g);
+        else phase_flip<W, 6>(p, b, smem_raw, g);
         if (!grid_barrier(st)) return;
-        phase_partition<W>(p, b);
+        phase_partition<W>(p, b, g);
         if (!grid_barrier(st)) return;
-        phase_merge<W>(p, b, smem_raw, true);
+        phase_merge<W>(p, b, smem_raw, true, g);
         if (!grid_barrier(st)) return;
         // written only by the committing CTA before this barrier: uniform
         if (*reinterpret_cast<volatile unsigned*>(&st->stop)) return;
     }
+}
+
+// ================================================================= batched
+// Many independent maps ("items": powder orientations, disorder realizations,
+// served requests) advanced by one launch: each item is owned by one
+// thread-block cluster of G CTAs (G = 1, 2, 4 or 8, chosen by the autotuner),
+// which runs the item's whole rotation list with the same phases as above.
+// Phases are separated by the hardware cluster barrier (release/acquire at
+// cluster scope; a cluster of one CTA is a plain CTA barrier), so no software
+// spin-wait is involved.  Items finish independently; the hardware scheduler
+// starts the next clusters as SMs free up.
+struct BatchItem {
+    const RotParams* ps;   // this item's rotation list (device memory)
+    unsigned rotations;
+    unsigned active;       // 0: skip (finished or failed item)
+    uint64_t* keys[3];
+    double* vals[3];
+    int x, y, z;
+    int final_buf;         // buffer holding the map after the rotations
+    unsigned n_spins;
+    Buffers scratch;       // the item's own fk..st, cap
+};
+
+__device__ __forceinline__ void cluster_barrier() {
+    __threadfence();
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+                 ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+    unsigned n;
+    asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+    return n;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kP3Block, 2) k_batch(const BatchItem* items, const unsigned* ids) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Grid g{cluster_rank(), cluster_size()};
+    const BatchItem& it = items[ids[blockIdx.x / g.ncta]];
+    if (!it.active) return;  // uniform across the cluster
+    DeviceState* st = it.scratch.st;
+    for (unsigned r = 0; r < it.rotations; ++r) {
+        const RotParams& p = it.ps[r];
+        const int in = r == 0 ? it.x : ((r - 1) % 2 == 0 ? it.y : it.z);
+        const int out = r % 2 == 0 ? it.y : it.z;
+        Buffers b = it.scratch;
+        b.in_keys = it.keys[in];
+        b.in_vals = it.vals[in];
+        b.out_keys = it.keys[out];
+        b.out_vals = it.vals[out];
+        if (r == 0) {
+            phase_classify<W>(p, b, g);
+            cluster_barrier();
+        }
+        if (p.nth <= 4) phase_flip<W, 4>(p, b, smem_raw, g);
+        else phase_flip<W, 6>(p, b, smem_raw, g);
+        cluster_barrier();
+        phase_partition<W>(p, b, g);
+        cluster_barrier();
+        phase_merge<W>(p, b, smem_raw, true, g);
+        cluster_barrier();
+        if (__ldcg(&st->stop)) break;  // written by the committing CTA before the barrier
+    }
+}
+
+// Per item, the coefficient of each weight-one key `pauli` at site s after a
+// batched step (0 if absent): out[item * 128 + s].  One CTA per item.
+template <int W>
+__global__ void k_batch_readout(const BatchItem* items, const unsigned* ids, unsigned pauli,
+                                double* out) {
+    const unsigned item = ids[blockIdx.x];
+    const BatchItem& it = items[item];
+    const unsigned s = threadIdx.x;
+    double v = 0.0;
+    if (it.active && s < it.n_spins) {
+        const uint64_t* keys = it.keys[it.final_buf];
+        const double* vals = it.vals[it.final_buf];
+        const unsigned long long len = __ldcg(&it.scratch.st->n);
+        Key<W> target;
+#pragma unroll
+        for (int w = 0; w < W; ++w) target.w[w] = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            if (w == (int)(s / 32)) target.w[w] = (uint64_t)pauli << (2 * (s % 32));
+        unsigned long long lo = 0, hi = len;
+        while (lo < hi) {
+            const unsigned long long mid = lo + (hi - lo) / 2;
+            if (key_less<W>(load_key<W>(keys, mid), target)) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < len && key_eq<W>(load_key<W>(keys, lo), target)) v = __ldcg(vals + lo);
+    }
+    if (s < 128) out[(size_t)item * 128 + s] = v;
 }
 
 }  // namespace tg

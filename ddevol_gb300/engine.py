@@ -23,7 +23,7 @@ import numpy as np
 from . import native
 from .native import CUDA_STATUS_NAMES, STATUS_NAMES, GbLedger, GbOptions, GbTerm
 
-__all__ = ["CudaBranchContext", "Engine", "DeviceMap", "options", "terms_array",
+__all__ = ["CudaBranchContext", "Engine", "DeviceMap", "Batch", "options", "terms_array",
            "STATUS_NAMES", "CUDA_STATUS_NAMES", "GbLedger"]
 
 
@@ -223,6 +223,105 @@ class DeviceMap:
     def close(self):
         if getattr(self, "ptr", None):
             self.lib.tpgp_gb_map_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent maps advanced together (tpgp_gb_batch)."""
+
+    def __init__(self, engine: Engine, n_spins_list):
+        self.engine = engine
+        self.lib = engine.lib
+        self.n_spins = [int(n) for n in n_spins_list]
+        arr = (C.c_size_t * len(self.n_spins))(*self.n_spins)
+        ptr = C.c_void_p()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_batch_create(engine.ptr, len(self.n_spins), arr, C.byref(ptr), err,
+                                           len(err))
+        if st:
+            raise RuntimeError(f"tpgp_gb_batch_create failed: {err.value.decode()}")
+        self.ptr = ptr
+        self._keep = {}
+
+    def __len__(self):
+        return len(self.n_spins)
+
+    def upload(self, item, keys, values):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_batch_upload(self.ptr, item, _u64p(keys), _f64p(values), len(values),
+                                           err, len(err))
+        if st:
+            raise ValueError(f"batch upload failed: {err.value.decode()}")
+
+    def set_terms(self, item, terms, dt, opts):
+        arr, count = terms_array(terms)
+        self._keep[item] = arr
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_batch_set_terms(self.ptr, item, arr, count, dt, C.byref(opts), err,
+                                              len(err))
+        if st:
+            raise ValueError(f"batch set_terms failed ({STATUS_NAMES[st]}): {err.value.decode()}")
+
+    def step(self, steps=1, record_fid=True):
+        fids = np.zeros((max(1, steps), len(self)), np.float64)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_batch_step(self.ptr, steps, _f64p(fids) if record_fid else None,
+                                         err, len(err))
+        if st:
+            raise RuntimeError(f"batch step failed: {err.value.decode()}")
+        return fids[:steps]
+
+    def autotune(self):
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_batch_autotune(self.ptr, err, len(err))
+        if st:
+            raise RuntimeError(f"autotune failed: {err.value.decode()}")
+        return {w: self.lib.tpgp_gb_batch_cluster(self.ptr, w) for w in (1, 2, 3, 4)}
+
+    def item_status(self, item):
+        return self.lib.tpgp_gb_batch_item_status(self.ptr, item)
+
+    def item_len(self, item):
+        return self.lib.tpgp_gb_batch_len(self.ptr, item)
+
+    def ledger(self, item):
+        led = GbLedger()
+        self.lib.tpgp_gb_batch_ledger(self.ptr, item, C.byref(led))
+        return led
+
+    def download(self, item):
+        n = self.item_len(item)
+        words = (self.n_spins[item] + 31) // 32
+        keys = np.zeros(max(1, n * words), np.uint64)
+        values = np.zeros(max(1, n), np.float64)
+        got = C.c_size_t()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_batch_download(self.ptr, item, _u64p(keys), _f64p(values), n,
+                                             C.byref(got), err, len(err))
+        if st:
+            raise RuntimeError(f"batch download failed: {err.value.decode()}")
+        return keys[:got.value * words], values[:got.value]
+
+    def last_elapsed_ms(self):
+        return self.lib.tpgp_gb_batch_last_elapsed_ms(self.ptr)
+
+    def last_terms(self):
+        return self.lib.tpgp_gb_batch_last_terms(self.ptr)
+
+    def last_launches(self):
+        return self.lib.tpgp_gb_batch_last_launches(self.ptr)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.tpgp_gb_batch_destroy(self.ptr)
             self.ptr = None
 
     def __del__(self):

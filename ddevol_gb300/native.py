@@ -98,6 +98,34 @@ def _bind(lib):
     lib.tpgp_gb_last_launches.argtypes = [C.c_void_p]
     lib.tpgp_gb_last_terms.restype = sz
     lib.tpgp_gb_last_terms.argtypes = [C.c_void_p]
+    lib.tpgp_gb_batch_create.restype = C.c_int
+    lib.tpgp_gb_batch_create.argtypes = [C.c_void_p, sz, P(sz), P(C.c_void_p), charp, sz]
+    lib.tpgp_gb_batch_destroy.argtypes = [C.c_void_p]
+    lib.tpgp_gb_batch_upload.restype = C.c_int
+    lib.tpgp_gb_batch_upload.argtypes = [C.c_void_p, sz, u64p, f64p, sz, charp, sz]
+    lib.tpgp_gb_batch_set_terms.restype = C.c_int
+    lib.tpgp_gb_batch_set_terms.argtypes = [C.c_void_p, sz, P(GbTerm), sz, C.c_double,
+                                            P(GbOptions), charp, sz]
+    lib.tpgp_gb_batch_step.restype = C.c_int
+    lib.tpgp_gb_batch_step.argtypes = [C.c_void_p, sz, f64p, charp, sz]
+    lib.tpgp_gb_batch_autotune.restype = C.c_int
+    lib.tpgp_gb_batch_autotune.argtypes = [C.c_void_p, charp, sz]
+    lib.tpgp_gb_batch_cluster.restype = C.c_int
+    lib.tpgp_gb_batch_cluster.argtypes = [C.c_void_p, sz]
+    lib.tpgp_gb_batch_item_status.restype = C.c_int
+    lib.tpgp_gb_batch_item_status.argtypes = [C.c_void_p, sz]
+    lib.tpgp_gb_batch_len.restype = sz
+    lib.tpgp_gb_batch_len.argtypes = [C.c_void_p, sz]
+    lib.tpgp_gb_batch_ledger.restype = C.c_int
+    lib.tpgp_gb_batch_ledger.argtypes = [C.c_void_p, sz, P(GbLedger)]
+    lib.tpgp_gb_batch_download.restype = C.c_int
+    lib.tpgp_gb_batch_download.argtypes = [C.c_void_p, sz, u64p, f64p, sz, P(sz), charp, sz]
+    lib.tpgp_gb_batch_last_elapsed_ms.restype = C.c_double
+    lib.tpgp_gb_batch_last_elapsed_ms.argtypes = [C.c_void_p]
+    lib.tpgp_gb_batch_last_terms.restype = sz
+    lib.tpgp_gb_batch_last_terms.argtypes = [C.c_void_p]
+    lib.tpgp_gb_batch_last_launches.restype = sz
+    lib.tpgp_gb_batch_last_launches.argtypes = [C.c_void_p]
     lib.tpgp_gb_set_profiling.argtypes = [C.c_void_p, C.c_int]
     lib.tpgp_gb_kernel_profile.argtypes = [C.c_void_p, f64p, P(sz)]
     return lib

@@ -155,6 +155,52 @@ size_t tpgp_gb_last_terms(const tpgp_gb_map *map);
 void tpgp_gb_set_profiling(tpgp_gb_map *map, int on);
 void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t *launches);
 
+/* Batched maps (no reference counterpart; the reference runs independent
+ * solves as separate processes, scripts/campaign.sh).  A batch holds
+ * n_items independent maps (powder orientations, disorder realizations,
+ * served requests), each with its own spins, terms, dt and options, and
+ * advances all of them by one clustered launch per Strang step and key width:
+ * every item is owned by one thread-block cluster of G CTAs that runs the
+ * item's whole rotation list, and the step's transfers and launches are
+ * replayed from a CUDA graph.  Results per item are those of
+ * tpgp_gb_strang_step on that item alone (keys, values, FID bitwise).
+ * Items fail independently: item_status() is the tpgp_status of an item's
+ * failed step (the item then stays at its last accepted step and is
+ * skipped), 0 while healthy. */
+typedef struct tpgp_gb_batch tpgp_gb_batch;
+tpgp_gb_status tpgp_gb_batch_create(tpgp_gb_context *context, size_t n_items,
+                                    const size_t *n_spins, tpgp_gb_batch **batch, char *error,
+                                    size_t error_capacity);
+void tpgp_gb_batch_destroy(tpgp_gb_batch *batch);
+tpgp_gb_status tpgp_gb_batch_upload(tpgp_gb_batch *batch, size_t item, const uint64_t *keys,
+                                    const double *values, size_t len, char *error,
+                                    size_t error_capacity);
+/* The item's Hamiltonian terms, time step and options (as tpgp_gb_strang_step). */
+tpgp_gb_status tpgp_gb_batch_set_terms(tpgp_gb_batch *batch, size_t item,
+                                       const tpgp_gb_term *terms, size_t count, double dt,
+                                       const tpgp_gb_options *options, char *error,
+                                       size_t error_capacity);
+/* `steps` Strang steps of every healthy item; fid_sums (steps x n_items, may
+ * be NULL) receives each item's single_sum(X) after each step (NaN for a
+ * failed item).  Returns a non-OK status only for a device failure. */
+tpgp_gb_status tpgp_gb_batch_step(tpgp_gb_batch *batch, size_t steps, double *fid_sums,
+                                  char *error, size_t error_capacity);
+/* Picks, per key width, the cluster size G in {1, 2, 4, 8} with the fastest
+ * trial step on the current maps (trial steps are not committed). */
+tpgp_gb_status tpgp_gb_batch_autotune(tpgp_gb_batch *batch, char *error, size_t error_capacity);
+int tpgp_gb_batch_cluster(const tpgp_gb_batch *batch, size_t n_words);
+int tpgp_gb_batch_item_status(const tpgp_gb_batch *batch, size_t item);
+size_t tpgp_gb_batch_len(const tpgp_gb_batch *batch, size_t item);
+tpgp_gb_status tpgp_gb_batch_ledger(const tpgp_gb_batch *batch, size_t item,
+                                    tpgp_gb_ledger *ledger);
+tpgp_gb_status tpgp_gb_batch_download(const tpgp_gb_batch *batch, size_t item, uint64_t *keys,
+                                      double *values, size_t capacity, size_t *len, char *error,
+                                      size_t error_capacity);
+/* Device time (ms), input terms and launches of the last batch_step call. */
+double tpgp_gb_batch_last_elapsed_ms(const tpgp_gb_batch *batch);
+size_t tpgp_gb_batch_last_terms(const tpgp_gb_batch *batch);
+size_t tpgp_gb_batch_last_launches(const tpgp_gb_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif
