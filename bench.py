@@ -191,6 +191,19 @@ class Dist:
 
 
 # ------------------------------------------------------------- CPU samples
+class L2Flush:
+    """Writes a 512 MB device buffer (four times the 129 MB L2) and waits."""
+
+    def __init__(self, device):
+        import torch
+        self.torch = torch
+        self.buf = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+
+    def __call__(self):
+        self.buf.fill_(1)
+        self.torch.cuda.synchronize()
+
+
 def cpu_sample(keys, vals, n, terms, dt, threshold, budget_s, cores):
     """Rotations of one Strang step (forward order) on the CPU oracle, from the
     given state, until the wall budget is spent.  Returns (terms, seconds,
@@ -285,16 +298,24 @@ def run_gb300(args, dist):
     sampler.start()
     time.sleep(0.3)
     n_before = len(m)
+    flush = L2Flush(dist.local_rank)
+    ms, terms_done, launches, fids = 0.0, 0, 0, []
+    flush()
     dist.barrier()
     profiler_range(True)
-    st, fids, led, msg = m.evolve(terms, cfg["dt"], args.steps, opts, led)
+    for _ in range(args.steps):
+        # one Strang step per call, device-timed on the engine's stream; the
+        # L2 is flushed between timed steps (outside the timed interval)
+        st, f, led, msg = m.evolve(terms, cfg["dt"], 1, opts, led)
+        if st:
+            raise RuntimeError(msg)
+        ms += m.last_elapsed_ms()
+        terms_done += m.last_terms()
+        launches += m.last_launches()
+        fids.extend(f)
+        flush()
     profiler_range(False)
-    if st:
-        raise RuntimeError(msg)
     dist.barrier()
-    ms = m.last_elapsed_ms()
-    terms_done = m.last_terms()
-    launches = m.last_launches()
     n_after = len(m)
     clocks = sampler.stop()
     t_max = dist.reduce(ms / 1e3, "max")
@@ -391,9 +412,9 @@ def run_gb300(args, dist):
             "rotations_per_step": 2 * len(terms), "setup_steps": setup_steps,
             "window_start_step": setup_steps + args.warmup,
             "terms_at_window_start": n_before, "terms_after_window": n_after,
-            "ledger": "exact (sequential)" if args.exact_ledger else "bound (tree)",
-            "l2": f"map {n_before * (8 * words + 8) / 1e6:.0f} MB per buffer; no flush "
-                  f"(L2 129 MB)",
+            "ledger": "exact (sequential)" if args.exact_ledger else "bound (fixed-point)",
+            "l2": f"map {n_before * (8 * words + 8) / 1e6:.1f} MB per buffer; L2 flushed "
+                  f"(512 MB write) between timed steps",
             "parallelism": f"replicas x{dist.world}"},
         "e2e": e2e,
         "gpu_launches": launches,
@@ -441,14 +462,19 @@ def run_powder(args, dist):
     sampler = ClockSampler(physical_gpu_index(dist.local_rank))
     sampler.start()
     time.sleep(0.3)
+    flush = L2Flush(dist.local_rank)
+    ms, terms_done, launches = 0.0, 0, 0
+    flush()
     dist.barrier()
     profiler_range(True)
-    batch.step(args.steps, record_fid=True)
+    for _ in range(args.steps):
+        batch.step(1, record_fid=True)
+        ms += batch.last_elapsed_ms()
+        terms_done += batch.last_terms()
+        launches += batch.last_launches()
+        flush()
     profiler_range(False)
     dist.barrier()
-    ms = batch.last_elapsed_ms()
-    terms_done = batch.last_terms()
-    launches = batch.last_launches()
     clocks = sampler.stop()
     t_max = dist.reduce(ms / 1e3, "max")
     terms_all = dist.reduce(float(terms_done), "sum")
@@ -483,10 +509,103 @@ def run_powder(args, dist):
                    "terms_per_item_after": {"min": int(min(sizes)), "median": int(np.median(sizes)),
                                             "max": int(max(sizes))},
                    "cluster_ctas_per_item": clusters, "failed_items": failed,
-                   "ledger": "bound (fixed-point)", "parallelism": f"replicas x{dist.world}"},
+                   "ledger": "bound (fixed-point)",
+                   "l2": "L2 flushed (512 MB write) between timed steps",
+                   "parallelism": f"replicas x{dist.world}"},
         "item_step_solves_per_s": len(items) * args.steps / t_max,
         "full_solve": full,
         "gpu_launches": launches, "clocks": clocks,
+    }
+
+
+SERVE = dict(dt=0.01, cutoff=3, steps=(20, 80), slots=(32, 64, 64), seed=20261203,
+             target_busy=0.8, memory_budget=200 << 30,
+             label="Poisson stream of FID solves: ring or chain (p=1/2), N uniform in {16..96} "
+                   "(key widths 1-3 words), d=g/r^3 with g~N(1,0.1) per pair, pairs within "
+                   "ring/chain distance 3, threshold log-uniform in [1e-6,1e-4], steps uniform "
+                   "in {20..80}, dt=0.01, X_0; slots 32/64/64 of 32/64/96 spins")
+
+
+def serve_requests(count, rate, seed):
+    from ddevol_gb300.engine import options
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=count)) if rate > 0 else np.zeros(count)
+    reqs = []
+    for k in range(count):
+        n, terms, thr, steps, dt = H.serving_request(rng, steps_range=SERVE["steps"],
+                                                     cutoff=SERVE["cutoff"], dt=SERVE["dt"])
+        keys, vals = H.single_site_operator(n, 0)
+        reqs.append(dict(arrival=float(arrivals[k]), n_spins=n, terms=terms, dt=dt, steps=steps,
+                         options=options(thr, exact_ledger=False), keys=keys, values=vals))
+    return reqs
+
+
+def run_serve(args, dist):
+    """Serving form: a Poisson stream of FID solves through tpgp_gb_serve
+    (continuous batching over the batched kernel).  The arrival rate is
+    calibrated in two short runs so that the device is busy about 80% of
+    the wall time; latency is finish minus arrival."""
+    from ddevol_gb300.engine import Engine
+    eng = Engine(dist.local_rank)
+    seed = SERVE["seed"] + 7919 * dist.rank
+    slots, budget = SERVE["slots"], SERVE["memory_budget"]
+    # saturation: every request present at t = 0
+    burst = serve_requests(96, 0.0, seed + 1)
+    _, _, st0 = eng.serve(burst, slots=slots, memory_budget=budget, record_fid=False)
+    mu = len(burst) / st0["wall_seconds"]
+    rate = SERVE["target_busy"] * mu
+    calib = []
+    for _ in range(2):
+        trial = serve_requests(max(48, int(rate * 8)), rate, seed + 2 + len(calib))
+        _, _, st1 = eng.serve(trial, slots=slots, memory_budget=budget, record_fid=False)
+        busy = st1["busy_seconds"] / st1["wall_seconds"]
+        calib.append({"rate": rate, "requests": len(trial), "busy": busy})
+        rate *= SERVE["target_busy"] / max(busy, 1e-3)
+    count = int(min(10000, max(64, rate * args.serve_seconds)))
+    reqs = serve_requests(count, rate, seed)
+    sampler = ClockSampler(physical_gpu_index(dist.local_rank))
+    sampler.start()
+    time.sleep(0.3)
+    dist.barrier()
+    profiler_range(True)
+    resp, fids, st = eng.serve(reqs, slots=slots, memory_budget=budget)
+    profiler_range(False)
+    dist.barrier()
+    clocks = sampler.stop()
+    lat = np.array([r["finished"] - q["arrival"] for r, q in zip(resp, reqs)])
+    wait = np.array([r["admitted"] - q["arrival"] for r, q in zip(resp, reqs)])
+    failed = sum(1 for r in resp if r["status"])
+    # replay a few requests alone: the served FIDs must be bitwise the same
+    rng = np.random.default_rng(seed + 99)
+    picks = sorted(rng.choice(count, size=min(4, count), replace=False).tolist())
+    same = True
+    for r in picks:
+        _, f1, _ = eng.serve([dict(reqs[r], arrival=0.0)], slots=(1, 1, 1), memory_budget=budget)
+        same &= bool(np.array_equal(f1[0].view(np.uint64), fids[r].view(np.uint64)))
+    eng.close()
+    wall = dist.reduce(st["wall_seconds"], "max")
+    terms_all = dist.reduce(float(st["terms"]), "sum")
+    solves_all = dist.reduce(float(count - failed), "sum")
+    widths = np.array([(q["n_spins"] + 31) // 32 for q in reqs])
+    return {
+        "metric": METRIC, "value": terms_all / wall, "unit": METRIC, "n_gpus": dist.world,
+        "steps": int(st["ticks"]), "warmup": len(calib) + 1,
+        "ms_per_step": st["wall_seconds"] * 1e3 / max(1, st["ticks"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded request stream; no dataset)",
+        "config": {"workload": "serve_stream", "description": SERVE["label"], "requests": count,
+                   "rate_per_s": rate, "width_mix": {w: int((widths == w).sum()) for w in (1, 2, 3)},
+                   "calibration": calib, "ledger": "bound (fixed-point)",
+                   "parallelism": f"replicas x{dist.world}"},
+        "serve": {"solves_per_s": solves_all / wall, "latency_s_p50": float(np.percentile(lat, 50)),
+                  "latency_s_p99": float(np.percentile(lat, 99)),
+                  "queue_s_p50": float(np.percentile(wait, 50)),
+                  "queue_s_p99": float(np.percentile(wait, 99)),
+                  "busy_fraction": st["busy_seconds"] / st["wall_seconds"],
+                  "wall_s": st["wall_seconds"], "ticks": int(st["ticks"]),
+                  "max_active": int(st["max_active"]), "failed": failed,
+                  "replayed_alone_bitwise": {"requests": picks, "equal": same}},
+        "gpu_launches": int(st["launches"]), "clocks": clocks,
     }
 
 
@@ -540,11 +659,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--config", choices=sorted(CONFIGS) + ["powder"], default="ring64")
+    ap.add_argument("--config", choices=sorted(CONFIGS) + ["powder", "serve"], default="ring64")
     ap.add_argument("--full-solve", action="store_true",
                     help="powder: continue to 300 steps and report FID solves/s")
     ap.add_argument("--full-budget", type=float, default=120.0,
                     help="powder: wall-second budget for --full-solve")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="serve: length of the measured request stream at the calibrated rate")
     ap.add_argument("--target-terms", type=float, default=1e5,
                     help="set-up evolves until the map holds this many terms")
     ap.add_argument("--max-setup-steps", type=int, default=400)
@@ -559,6 +680,8 @@ def main():
     try:
         if args.config == "powder":
             line = run_powder(args, dist)
+        elif args.config == "serve":
+            line = run_serve(args, dist)
         elif args.impl == "reference":
             line = run_reference(args, dist)
         else:

@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_native")
 LIB = os.path.join(OUT_DIR, "libtpgp_gb300.so")
-UNITS = ["branch_abi.cu", "engine.cu"]
+UNITS = ["branch_abi.cu", "engine.cu", "serve.cu"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

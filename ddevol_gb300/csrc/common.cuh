@@ -18,6 +18,18 @@
 
 namespace tg {
 
+// ------------------------------------------------ programmatic dependent launch
+// A kernel launched with programmatic stream serialization may be scheduled
+// while its predecessor on the stream is still running.  It waits here for
+// the predecessor's completion (and the visibility of its memory) before it
+// touches any state, then lets its own successor be scheduled, so only the
+// launch latency overlaps, never the work.  Launched without the attribute,
+// both instructions return at once.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- status bits
 enum : unsigned {
     ST_NUMERIC = 1u,    // nonfinite branch value or merged sum -> ENUMERIC

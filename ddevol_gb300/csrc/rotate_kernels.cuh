@@ -218,68 +218,97 @@ __device__ void phase_classify(const RotParams& p, const Buffers& b, Grid g) {
 
 template <int W>
 __global__ void __launch_bounds__(kP1Block) k_classify(RotParams p, Buffers b) {
+    pdl_enter();
     phase_classify<W>(p, b, whole_grid());
 }
 
 // ======================================================================= P2
-// Galloping search over the anticommuting sequence A (A[y] = fk[y] xor M) for
-// the start of the run of elements that share all bits >= theta with A[from]
-// (backward = true), or for the first element after that run (forward).
+// Warp-cooperative search over the anticommuting sequence A (A[y] = fk[y]
+// xor M) for the start of the run of elements that share all bits >= theta
+// with A[from] (backward = true), or for the first element after that run
+// (forward; a if the run reaches the end).  The predicate is monotone on each
+// side of `from`.  Each round the 32 lanes probe 32 positions: spaced by a
+// step that grows 32x per round while the run continues, then evenly inside
+// the bracketing interval, which shrinks 32x per round; so a run of length L
+// costs ~2 log_32(L) dependent loads.  Every lane of the (converged) warp
+// calls it and gets the same result.
 template <int W>
-__device__ unsigned long long run_edge(const uint64_t* fk, const Key<W>& M,
-                                       unsigned long long a, unsigned long long from,
-                                       int theta, bool backward) {
+__device__ unsigned long long run_edge_warp(const uint64_t* fk, const Key<W>& M,
+                                            unsigned long long a, unsigned long long from,
+                                            int theta, bool backward) {
+    const long long lane = (long long)lane_id();
     const Key<W> target = key_high<W>(key_xor<W>(load_key_coherent<W>(fk, from), M), theta);
-    auto same = [&](unsigned long long y) {
-        return key_eq<W>(key_high<W>(key_xor<W>(load_key_coherent<W>(fk, y), M), theta), target);
+    auto same = [&](long long y) {
+        return key_eq<W>(key_high<W>(key_xor<W>(load_key_coherent<W>(fk, (size_t)y), M), theta),
+                         target);
     };
+    const long long n = (long long)a;
     if (backward) {
-        // find the smallest y <= from with same(y); same(from) holds
-        unsigned long long good = from, step = 1;
-        unsigned long long bad_pos = ~0ull;  // ~0 = "before 0"
+        // smallest y <= from with same(y); bracket (bad, good]: !same(bad) (or bad = -1), same(good)
+        long long good = (long long)from, bad = -1, step = 1;
         while (true) {
-            if (good < step) {
-                if (same(0)) return 0;
-                bad_pos = 0;
+            const long long y = good - (lane + 1) * step;
+            const unsigned fails = __ballot_sync(0xffffffffu, !(y >= 0 && same(y)));
+            if (fails) {
+                const long long l = __ffs(fails) - 1;
+                bad = max(-1ll, good - (l + 1) * step);
+                good -= l * step;
                 break;
             }
-            const unsigned long long y = good - step;
-            if (same(y)) {
-                good = y;
-                step <<= 1;
+            good -= 32 * step;
+            step *= 32;
+        }
+        while (good - bad > 1) {
+            const long long c = good - bad - 1;
+            const long long y = c <= 32 ? bad + 1 + lane : bad + 1 + (lane * c) / 32;
+            const bool in = lane < c || c > 32;
+            const unsigned hits = __ballot_sync(0xffffffffu, in && same(y));
+            if (!hits) {
+                if (c <= 32) break;
+                bad = __shfl_sync(0xffffffffu, y, 31);
             } else {
-                bad_pos = y;
-                break;
+                const int f = __ffs(hits) - 1;
+                const long long yf = __shfl_sync(0xffffffffu, y, f);
+                const long long yp = __shfl_sync(0xffffffffu, y, f > 0 ? f - 1 : 0);
+                good = yf;
+                if (c <= 32) break;
+                if (f > 0) bad = yp;
             }
         }
-        // invariant: !same(bad_pos), same(good), bad_pos < good
-        while (good - bad_pos > 1) {
-            const unsigned long long mid = bad_pos + (good - bad_pos) / 2;
-            if (same(mid)) good = mid;
-            else bad_pos = mid;
-        }
-        return good;
-    } else {
-        // find the smallest y > from with !same(y), or a
-        unsigned long long good = from, step = 1, bad_pos = a;
-        while (true) {
-            const unsigned long long y = good + step;
-            if (y >= a) break;
-            if (same(y)) {
-                good = y;
-                step <<= 1;
-            } else {
-                bad_pos = y;
-                break;
-            }
-        }
-        while (bad_pos - good > 1) {
-            const unsigned long long mid = good + (bad_pos - good) / 2;
-            if (same(mid)) good = mid;
-            else bad_pos = mid;
-        }
-        return bad_pos;
+        return (unsigned long long)good;
     }
+    // smallest y > from with !same(y), or a; bracket [good, bad): same(good), !same(bad) (or bad = a)
+    long long good = (long long)from, bad = n, step = 1;
+    while (true) {
+        const long long y = good + (lane + 1) * step;
+        const unsigned fails = __ballot_sync(0xffffffffu, !(y < n && same(y)));
+        if (fails) {
+            const long long l = __ffs(fails) - 1;
+            bad = min(n, good + (l + 1) * step);
+            good += l * step;
+            break;
+        }
+        good += 32 * step;
+        step *= 32;
+    }
+    while (bad - good > 1) {
+        const long long c = bad - good - 1;
+        const long long y = c <= 32 ? good + 1 + lane : good + 1 + (lane * c) / 32;
+        const bool in = lane < c || c > 32;
+        const unsigned miss = __ballot_sync(0xffffffffu, in && !same(y));
+        if (!miss) {
+            if (c <= 32) break;
+            good = __shfl_sync(0xffffffffu, y, 31);
+        } else {
+            const int f = __ffs(miss) - 1;
+            const long long yf = __shfl_sync(0xffffffffu, y, f);
+            const long long yp = __shfl_sync(0xffffffffu, y, f > 0 ? f - 1 : 0);
+            bad = yf;
+            if (c <= 32) break;
+            if (f > 0) good = yp;
+        }
+    }
+    return (unsigned long long)bad;
 }
 
 // NT: compile-time bound on the number of digit-boundary thresholds (4 when
@@ -317,20 +346,20 @@ __device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* 
             for (int w = 0; w < W; ++w) s_keys[(size_t)e * W + w] = k.w[w];
             s_vals[e] = __ldcg(b.fv + x0 + e);
         }
-        // run edges outside the tile for every threshold (galloping searches),
-        // as offsets from x0
-        if (threadIdx.x < 2 * nth) {
-            const int q = threadIdx.x % nth;
-            if (threadIdx.x < nth) {
+        // run edges outside the tile for every threshold (one warp per
+        // search), as offsets from x0
+        for (int sq = (int)warp; sq < 2 * nth; sq += kP2Block / 32) {
+            const int q = sq % nth;
+            if (sq < nth) {
                 // last y < x0 with bl(y) >= th[q]: start of the run holding x0-1
-                s_gprev[q] = x0 == 0 ? kNone
-                                     : (int)((long long)run_edge<W>(b.fk, M, a, x0 - 1, p.th[q], true) -
-                                             (long long)x0);
+                const long long r =
+                    x0 == 0 ? 0 : (long long)run_edge_warp<W>(b.fk, M, a, x0 - 1, p.th[q], true);
+                if (lane == 0) s_gprev[q] = x0 == 0 ? kNone : (int)(r - (long long)x0);
             } else {
                 // first y >= x1 with bl(y) >= th[q] (a if none)
                 const unsigned long long g =
-                    x1 >= a ? a : max(x1, run_edge<W>(b.fk, M, a, x1 - 1, p.th[q], false));
-                s_gnext[q] = (int)((long long)g - (long long)x0);
+                    x1 >= a ? a : max(x1, run_edge_warp<W>(b.fk, M, a, x1 - 1, p.th[q], false));
+                if (lane == 0) s_gnext[q] = (int)((long long)g - (long long)x0);
             }
         }
         __syncthreads();
@@ -481,6 +510,7 @@ __device__ void phase_flip(const RotParams& p, const Buffers& b, unsigned char* 
 template <int W, int NT>
 __global__ void __launch_bounds__(kP2Block) k_flip_sort(RotParams p, Buffers b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     phase_flip<W, NT>(p, b, smem_raw, whole_grid());
 }
 
@@ -530,6 +560,7 @@ __device__ void phase_partition(const RotParams& p, const Buffers& b, Grid g) {
 
 template <int W>
 __global__ void k_partition(RotParams p, Buffers b) {
+    pdl_enter();
     phase_partition<W>(p, b, whole_grid());
 }
 
@@ -948,6 +979,7 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
 template <int W>
 __global__ void __launch_bounds__(kP3Block, 3) k_merge(RotParams p, Buffers b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     phase_merge<W>(p, b, smem_raw, false, whole_grid());
 }
 

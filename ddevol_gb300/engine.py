@@ -21,7 +21,8 @@ import ctypes as C
 import numpy as np
 
 from . import native
-from .native import CUDA_STATUS_NAMES, STATUS_NAMES, GbLedger, GbOptions, GbTerm
+from .native import (CUDA_STATUS_NAMES, STATUS_NAMES, GbLedger, GbOptions, GbRequest,
+                     GbResponse, GbServeStats, GbTerm)
 
 __all__ = ["CudaBranchContext", "Engine", "DeviceMap", "Batch", "options", "terms_array",
            "STATUS_NAMES", "CUDA_STATUS_NAMES", "GbLedger"]
@@ -111,6 +112,41 @@ class Engine:
                 m.close()
                 raise ValueError(f"upload failed ({STATUS_NAMES[st]}): {msg}")
         return m
+
+    def serve(self, requests, slots=(8, 8, 8), memory_budget=64 << 30, record_fid=True):
+        """Serves FID-solve requests with continuous batching (tpgp_gb_serve).
+
+        requests: dicts with arrival (s), n_spins, terms, dt, steps, options,
+        keys, values.  Returns (responses as dicts, per-request FID arrays,
+        stats as a dict)."""
+        n = len(requests)
+        reqs = (GbRequest * max(1, n))()
+        keep = []
+        for r, q in enumerate(requests):
+            arr, count = terms_array(q["terms"])
+            keys = np.ascontiguousarray(q["keys"], dtype=np.uint64)
+            vals = np.ascontiguousarray(q["values"], dtype=np.float64)
+            keep += [arr, keys, vals]
+            reqs[r] = GbRequest(float(q["arrival"]), int(q["n_spins"]), arr, count, float(q["dt"]),
+                                int(q["steps"]), q["options"], _u64p(keys), _f64p(vals), len(vals))
+        total = sum(int(q["steps"]) for q in requests)
+        fids = np.zeros(max(1, total), np.float64)
+        resp = (GbResponse * max(1, n))()
+        slot_arr = (C.c_size_t * 3)(*slots)
+        stats = GbServeStats()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_serve(self.ptr, reqs, n, slot_arr, int(memory_budget),
+                                    _f64p(fids) if record_fid else None, resp, C.byref(stats), err,
+                                    len(err))
+        if st:
+            raise RuntimeError(f"serve failed ({STATUS_NAMES[st]}): {err.value.decode()}")
+        out, per, off = [], [], 0
+        for r, q in enumerate(requests):
+            x = resp[r]
+            out.append({name: getattr(x, name) for name, _ in GbResponse._fields_})
+            per.append(fids[off:off + int(q["steps"])].copy())
+            off += int(q["steps"])
+        return out, per, {name: getattr(stats, name) for name, _ in GbServeStats._fields_}
 
     def close(self):
         if self.ptr:
@@ -285,6 +321,17 @@ class Batch:
         if st:
             raise RuntimeError(f"autotune failed: {err.value.decode()}")
         return {w: self.lib.tpgp_gb_batch_cluster(self.ptr, w) for w in (1, 2, 3, 4)}
+
+    def set_cluster(self, n_words, base, terms_per_cta=0):
+        """Base cluster size and terms per CTA of the size rule for one key width."""
+        err = C.create_string_buffer(256)
+        st = self.lib.tpgp_gb_batch_set_cluster(self.ptr, n_words, base, terms_per_cta, err,
+                                                len(err))
+        if st:
+            raise ValueError(err.value.decode())
+
+    def max_cluster(self, n_words):
+        return self.lib.tpgp_gb_batch_max_cluster(self.ptr, n_words)
 
     def item_status(self, item):
         return self.lib.tpgp_gb_batch_item_status(self.ptr, item)

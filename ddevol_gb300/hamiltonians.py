@@ -189,3 +189,33 @@ def global_x_operator(n_spins: int):
         keys[s, s // 32] = np.uint64(X) << np.uint64(2 * (s % 32))
     order = sorted(range(n_spins), key=lambda r: tuple(int(x) for x in keys[r][::-1]))
     return keys[order].reshape(-1), np.ones(n_spins, np.float64)
+
+
+def _pairs_within(n: int, cutoff: int, periodic: bool):
+    """Pairs i < j (lexicographic) with ring (periodic) or chain distance <= cutoff."""
+    out = []
+    for i in range(n):
+        js = set(range(i + 1, min(n, i + cutoff + 1)))
+        if periodic:
+            js.update(range(max(i + 1, n - cutoff + i), n))
+        out += [(i, j) for j in sorted(js)]
+    return out
+
+
+def serving_request(rng, steps_range=(20, 80), cutoff=3, dt=0.01):
+    """One FID-solve request of the serving stream: a ring or an open chain
+    (p = 1/2) of N uniform in {16..96} spins, couplings d = g_ij / r^3 with a
+    Gaussian disorder factor g ~ N(1, 0.1) per pair, pairs up to ring/chain
+    distance ``cutoff`` (the term list equals ``ring_all_pairs`` /
+    ``chain_all_pairs`` with that cutoff), threshold log-uniform in
+    [1e-6, 1e-4], X on site 0.  Returns (n, terms, threshold, steps, dt)."""
+    n = int(rng.integers(16, 97))
+    scale = rng.normal(1.0, 0.1, size=(n, n))
+    ring = bool(rng.random() < 0.5)
+    terms = []
+    for i, j in _pairs_within(n, cutoff, ring):
+        d = 1.0 / (chord(n, i, j) ** 3 if ring else float(j - i) ** 3)
+        terms += edge_terms(i, j, 2 * (d * float(scale[i, j])))
+    threshold = float(10.0 ** rng.uniform(-6, -4))
+    steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+    return n, terms, threshold, steps, dt

@@ -43,6 +43,31 @@ class GbOptions(C.Structure):
                 ("max_drop_l2", C.c_double), ("exact_ledger", C.c_int), ("use_graphs", C.c_int)]
 
 
+class GbRequest(C.Structure):
+    """tpgp_gb_request (include/tpgp_gb300.h)."""
+
+    _fields_ = [("arrival", C.c_double), ("n_spins", C.c_size_t), ("terms", C.POINTER(GbTerm)),
+                ("count", C.c_size_t), ("dt", C.c_double), ("steps", C.c_size_t),
+                ("options", GbOptions), ("keys", C.POINTER(C.c_uint64)),
+                ("values", C.POINTER(C.c_double)), ("len", C.c_size_t)]
+
+
+class GbResponse(C.Structure):
+    """tpgp_gb_response (include/tpgp_gb300.h)."""
+
+    _fields_ = [("admitted", C.c_double), ("finished", C.c_double), ("status", C.c_int),
+                ("slot", C.c_size_t), ("slot_spins", C.c_size_t), ("peak_terms", C.c_size_t),
+                ("fid_last", C.c_double)]
+
+
+class GbServeStats(C.Structure):
+    """tpgp_gb_serve_stats (include/tpgp_gb300.h)."""
+
+    _fields_ = [("busy_seconds", C.c_double), ("wall_seconds", C.c_double),
+                ("ticks", C.c_ulonglong), ("terms", C.c_ulonglong), ("launches", C.c_ulonglong),
+                ("max_active", C.c_size_t)]
+
+
 def _bind(lib):
     P = C.POINTER
     u64p, f64p, charp = P(C.c_uint64), P(C.c_double), C.c_char_p
@@ -112,6 +137,10 @@ def _bind(lib):
     lib.tpgp_gb_batch_autotune.argtypes = [C.c_void_p, charp, sz]
     lib.tpgp_gb_batch_cluster.restype = C.c_int
     lib.tpgp_gb_batch_cluster.argtypes = [C.c_void_p, sz]
+    lib.tpgp_gb_batch_set_cluster.restype = C.c_int
+    lib.tpgp_gb_batch_set_cluster.argtypes = [C.c_void_p, sz, C.c_int, sz, charp, sz]
+    lib.tpgp_gb_batch_max_cluster.restype = C.c_int
+    lib.tpgp_gb_batch_max_cluster.argtypes = [C.c_void_p, sz]
     lib.tpgp_gb_batch_item_status.restype = C.c_int
     lib.tpgp_gb_batch_item_status.argtypes = [C.c_void_p, sz]
     lib.tpgp_gb_batch_len.restype = sz
@@ -126,6 +155,9 @@ def _bind(lib):
     lib.tpgp_gb_batch_last_terms.argtypes = [C.c_void_p]
     lib.tpgp_gb_batch_last_launches.restype = sz
     lib.tpgp_gb_batch_last_launches.argtypes = [C.c_void_p]
+    lib.tpgp_gb_serve.restype = C.c_int
+    lib.tpgp_gb_serve.argtypes = [C.c_void_p, P(GbRequest), sz, P(sz), sz, f64p, P(GbResponse),
+                                  P(GbServeStats), charp, sz]
     lib.tpgp_gb_set_profiling.argtypes = [C.c_void_p, C.c_int]
     lib.tpgp_gb_kernel_profile.argtypes = [C.c_void_p, f64p, P(sz)]
     return lib

@@ -159,10 +159,12 @@ void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t
  * solves as separate processes, scripts/campaign.sh).  A batch holds
  * n_items independent maps (powder orientations, disorder realizations,
  * served requests), each with its own spins, terms, dt and options, and
- * advances all of them by one clustered launch per Strang step and key width:
- * every item is owned by one thread-block cluster of G CTAs that runs the
- * item's whole rotation list, and the step's transfers and launches are
- * replayed from a CUDA graph.  Results per item are those of
+ * advances all of them by one clustered launch per Strang step, key width and
+ * cluster size: every item is owned by one thread-block cluster of G CTAs
+ * that runs the item's whole rotation list, and the step's transfers and
+ * launches are replayed from a CUDA graph.  G grows with the item's map (one
+ * CTA per 8192 terms by default, a power of two from the width's base size up
+ * to 16 where the device runs 16-CTA clusters, else 8).  Results per item are those of
  * tpgp_gb_strang_step on that item alone (keys, values, FID bitwise).
  * Items fail independently: item_status() is the tpgp_status of an item's
  * failed step (the item then stays at its last accepted step and is
@@ -182,13 +184,22 @@ tpgp_gb_status tpgp_gb_batch_set_terms(tpgp_gb_batch *batch, size_t item,
                                        size_t error_capacity);
 /* `steps` Strang steps of every healthy item; fid_sums (steps x n_items, may
  * be NULL) receives each item's single_sum(X) after each step (NaN for a
- * failed item).  Returns a non-OK status only for a device failure. */
+ * failed item and for an idle item: one with no terms or an empty map).
+ * Returns a non-OK status only for a device failure. */
 tpgp_gb_status tpgp_gb_batch_step(tpgp_gb_batch *batch, size_t steps, double *fid_sums,
                                   char *error, size_t error_capacity);
-/* Picks, per key width, the cluster size G in {1, 2, 4, 8} with the fastest
- * trial step on the current maps (trial steps are not committed). */
+/* Picks, per key width, the base cluster size G in {1, 2, 4, 8} with the
+ * fastest trial step on the current maps (trial steps are not committed).
+ * tpgp_gb_batch_cluster returns that base size. */
 tpgp_gb_status tpgp_gb_batch_autotune(tpgp_gb_batch *batch, char *error, size_t error_capacity);
 int tpgp_gb_batch_cluster(const tpgp_gb_batch *batch, size_t n_words);
+/* Sets the base cluster size (a power of two up to max_cluster) and the
+ * terms per CTA of the size rule (0: 8192) for one key width. */
+tpgp_gb_status tpgp_gb_batch_set_cluster(tpgp_gb_batch *batch, size_t n_words, int base,
+                                         size_t terms_per_cta, char *error,
+                                         size_t error_capacity);
+/* Largest cluster size the device runs for this key width (8 or 16). */
+int tpgp_gb_batch_max_cluster(const tpgp_gb_batch *batch, size_t n_words);
 int tpgp_gb_batch_item_status(const tpgp_gb_batch *batch, size_t item);
 size_t tpgp_gb_batch_len(const tpgp_gb_batch *batch, size_t item);
 tpgp_gb_status tpgp_gb_batch_ledger(const tpgp_gb_batch *batch, size_t item,
@@ -200,6 +211,52 @@ tpgp_gb_status tpgp_gb_batch_download(const tpgp_gb_batch *batch, size_t item, u
 double tpgp_gb_batch_last_elapsed_ms(const tpgp_gb_batch *batch);
 size_t tpgp_gb_batch_last_terms(const tpgp_gb_batch *batch);
 size_t tpgp_gb_batch_last_launches(const tpgp_gb_batch *batch);
+
+/* Serving (no reference counterpart).  A stream of FID solves served with
+ * continuous batching: requests are admitted, in arrival order, as soon as
+ * they have arrived, a slot of a large enough key width is free and the
+ * projected map memory of all admitted solves stays within memory_budget
+ * bytes (projection: the mean peak map size seen so far for that key width,
+ * 10^4 terms before any solve finished, times the arena bytes per term).
+ * Every tick advances all admitted solves by one Strang step in one batched
+ * launch; a solve leaves its slot after its last step and a waiting request
+ * takes it on the next tick.  Arrival times are seconds after the call
+ * starts (wall clock).  fids, when not NULL, receives each request's FID
+ * sums after each of its steps, requests concatenated in order.  Each
+ * solve's results are those of tpgp_gb_evolve on that request alone with
+ * n_spins rounded up to its slot's width (32, 64 or 96 spins). */
+typedef struct {
+    double arrival;
+    size_t n_spins;
+    const tpgp_gb_term *terms;
+    size_t count;
+    double dt;
+    size_t steps;
+    tpgp_gb_options options;
+    const uint64_t *keys; /* initial operator, n_spins-wide keys */
+    const double *values;
+    size_t len;
+} tpgp_gb_request;
+typedef struct {
+    double admitted, finished; /* seconds after the call started */
+    int status;                /* tpgp_status of the solve */
+    size_t slot, slot_spins, peak_terms;
+    double fid_last;
+} tpgp_gb_response;
+typedef struct {
+    double busy_seconds;      /* device time of all ticks */
+    double wall_seconds;      /* wall time of the call */
+    unsigned long long ticks; /* batched Strang steps */
+    unsigned long long terms; /* input terms summed over all rotations */
+    unsigned long long launches;
+    size_t max_active;        /* most solves admitted at once */
+} tpgp_gb_serve_stats;
+/* slots[w] = slots of key width w+1 words (w = 0, 1, 2: up to 32, 64, 96
+ * spins).  stats may be NULL. */
+tpgp_gb_status tpgp_gb_serve(tpgp_gb_context *context, const tpgp_gb_request *requests,
+                             size_t n_requests, const size_t slots[3], size_t memory_budget,
+                             double *fids, tpgp_gb_response *responses,
+                             tpgp_gb_serve_stats *stats, char *error, size_t error_capacity);
 
 #ifdef __cplusplus
 }

@@ -56,26 +56,37 @@ def test_batch_matches_single_solves(engine, exact):
     batch.close()
 
 
-def test_batch_cluster_sizes_agree(engine):
+@pytest.mark.parametrize("shape", ["autotune", (1, 0), (2, 0), (4, 64), (8, 32), (1, 16)])
+def test_batch_cluster_sizes_agree(engine, shape):
+    """Every cluster shape gives the single-solve result: autotuned base
+    sizes, forced base sizes, and small terms-per-CTA so that the size rule
+    puts the larger items on 8- and 16-CTA clusters."""
     items = powder_items(9, seed=5)
     dt = 0.02
-    results = []
-    for cluster in (None, 1, 2, 4, 8):
-        batch = Batch(engine, [n for n, _, _ in items])
-        for k, (n, terms, thr) in enumerate(items):
-            batch.upload(k, *H.single_site_operator(n, 0))
-            batch.set_terms(k, terms, dt, options(thr, exact_ledger=False))
-        batch.step(3)
-        if cluster is None:
-            chosen = batch.autotune()
-            assert chosen[1] in (1, 2, 4, 8)
-        batch.step(3)
-        results.append([batch.download(k) for k in range(len(items))])
-        batch.close()
-    base = results[0]
-    for other in results[1:]:
-        for (k1, v1), (k2, v2) in zip(base, other):
-            assert np.array_equal(k1, k2) and np.array_equal(bits(v1), bits(v2))
+    batch = Batch(engine, [n for n, _, _ in items])
+    for k, (n, terms, thr) in enumerate(items):
+        batch.upload(k, *H.single_site_operator(n, 0))
+        batch.set_terms(k, terms, dt, options(thr, exact_ledger=False))
+    if shape != "autotune":
+        base, per_cta = shape
+        for w in (1, 2):
+            batch.set_cluster(w, min(base, batch.max_cluster(w)), per_cta)
+    batch.step(3)
+    if shape == "autotune":
+        chosen = batch.autotune()
+        assert chosen[1] in (1, 2, 4, 8)
+    fids = batch.step(3)
+    assert batch.max_cluster(1) in (8, 16)
+    for k, (n, terms, thr) in enumerate(items):
+        m = engine.map(n, *H.single_site_operator(n, 0))
+        st, f1, _, msg = m.evolve(terms, dt, 6, options(thr, exact_ledger=False))
+        assert st == 0, msg
+        k1, v1 = m.download()
+        m.close()
+        k2, v2 = batch.download(k)
+        assert np.array_equal(k1, k2) and np.array_equal(bits(v1), bits(v2)), k
+        assert np.array_equal(bits(f1[3:]), bits(fids[:, k])), k
+    batch.close()
 
 
 def test_batch_item_failure_is_isolated(engine):

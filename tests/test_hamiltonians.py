@@ -44,3 +44,21 @@ def test_initial_operators():
     assert list(k) == [1, 0] and list(v) == [1.0]
     k, v = H.global_x_operator(6)
     assert list(k) == [1, 4, 16, 64, 256, 1024]
+
+
+def test_serving_request_matches_all_pairs_builders():
+    """The serving stream's fast pair walk builds the same term list as the
+    all-pairs builders with the same cutoff, for rings and chains."""
+    seen = set()
+    for seed in range(12):
+        rng = np.random.default_rng(seed)
+        n, terms, thr, steps, dt = H.serving_request(rng)
+        rng = np.random.default_rng(seed)
+        n2 = int(rng.integers(16, 97))
+        scale = rng.normal(1.0, 0.1, size=(n2, n2))
+        ring = bool(rng.random() < 0.5)
+        seen.add(ring)
+        build = H.ring_all_pairs if ring else H.chain_all_pairs
+        assert n == n2 and terms == build(n, scale=scale, cutoff=3)
+        assert 1e-6 <= thr <= 1e-4 and 20 <= steps <= 80 and dt == 0.01
+    assert seen == {True, False}

@@ -185,3 +185,24 @@ def test_persistent_step_kernel(golden_trajectories, oracle):
         eng.close()
     finally:
         os.environ.pop("TPGP_GB_PERSISTENT", None)
+
+
+def test_with_programmatic_launch(ring16_60_oracle):
+    """TPGP_GB_PDL=1 (programmatic dependent launch between the rotation
+    kernels) gives the same maps and FIDs as plain stream-ordered launches."""
+    import os
+    from ddevol_gb300.engine import Engine
+    terms, k0, v0, ok, ov, oled, fids_o = ring16_60_oracle
+    os.environ["TPGP_GB_PDL"] = "1"
+    try:
+        eng = Engine(0)
+        m = eng.map(16, k0, v0)
+        st, fids, _, msg = m.evolve(terms, 0.01, 60, options(1e-6, exact_ledger=False))
+        assert st == 0, msg
+        k, v = m.download()
+        m.close()
+        eng.close()
+        assert np.array_equal(k, ok) and np.array_equal(bits(v), bits(ov))
+        assert np.array_equal(bits(fids), bits(fids_o))
+    finally:
+        os.environ.pop("TPGP_GB_PDL", None)
