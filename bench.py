@@ -330,7 +330,8 @@ def run_gb300(args, dist):
     prof_terms = m.last_terms()
     n_p1 = len(m)
     m.set_profiling(False)
-    rot = prof["k_merge"][1] or 1
+    rot_kernel = "k_hash_rotate" if "k_hash_rotate" in prof else "k_merge"
+    rot = prof[rot_kernel][1] or 1
     total_ms = sum(v[0] for v in prof.values())
     dominant = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = prof[dominant]

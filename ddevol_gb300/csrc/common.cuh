@@ -38,6 +38,7 @@ enum : unsigned {
     ST_BUDGET = 8u,     // drop budget exceeded -> EBUDGET
     ST_TIMEOUT = 16u,   // a bounded wait gave up -> EBACKEND
     ST_ORDER = 32u,     // input keys not strictly ascending / padding bits -> EINVAL
+    ST_TABLE = 64u,     // hash-table step: probe bound hit; host enlarges the table and retries
 };
 
 // Maximum number of map terms a device map may hold (counts are packed

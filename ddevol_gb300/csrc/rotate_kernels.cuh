@@ -1082,6 +1082,7 @@ struct BatchItem {
     int x, y, z;
     int final_buf;         // buffer holding the map after the rotations
     unsigned n_spins;
+    unsigned table_slots;  // > 0: the step runs in a CTA-local hash table of this size
     Buffers scratch;       // the item's own fk..st, cap
 };
 

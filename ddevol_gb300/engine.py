@@ -245,16 +245,17 @@ class DeviceMap:
     def last_terms(self):
         return self.lib.tpgp_gb_last_terms(self.ptr)
 
-    KERNELS = ("k_classify", "k_flip_sort", "k_partition", "k_merge", "unused")
+    KERNELS = ("k_classify", "k_flip_sort", "k_partition", "k_merge", "k_hash_rotate",
+               "k_hash_build", "k_hash_chain_extract", "k_radix_sort")
 
     def set_profiling(self, on=True):
         self.lib.tpgp_gb_set_profiling(self.ptr, int(bool(on)))
 
     def kernel_profile(self):
-        ms = (C.c_double * 5)()
-        n = (C.c_size_t * 5)()
+        ms = (C.c_double * len(self.KERNELS))()
+        n = (C.c_size_t * len(self.KERNELS))()
         self.lib.tpgp_gb_kernel_profile(self.ptr, ms, n)
-        return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNELS) if k != "unused"}
+        return {k: (ms[i], n[i]) for i, k in enumerate(self.KERNELS) if n[i]}
 
     def close(self):
         if getattr(self, "ptr", None):

@@ -147,11 +147,13 @@ size_t tpgp_gb_last_launches(const tpgp_gb_map *map);
 size_t tpgp_gb_last_terms(const tpgp_gb_map *map);
 
 /* Per-kernel profile (no reference counterpart).  With profiling on, the
- * next calls launch without graphs and bracket every kernel with CUDA
- * events; kernel_profile then reports, for the rotation kernels in pipeline
- * order (classify, flip-sort, partition, merge; the fifth slot is unused),
- * the summed device milliseconds and launch counts since profiling was
- * switched on. */
+ * next calls launch without graphs and bracket the kernels with CUDA events;
+ * kernel_profile then fills TPGP_GB_PROFILE_SLOTS entries with the summed
+ * device milliseconds and launch counts since profiling was switched on:
+ * sorted path 0 classify, 1 flip-sort, 2 partition, 3 merge (each kernel
+ * bracketed); hash-table path 4 rotations, 5 table build, 6 commit chain and
+ * extraction, 7 radix sort (bracketed as groups). */
+#define TPGP_GB_PROFILE_SLOTS 8
 void tpgp_gb_set_profiling(tpgp_gb_map *map, int on);
 void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t *launches);
 

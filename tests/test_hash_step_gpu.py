@@ -1,0 +1,91 @@
+"""The hash-table Strang step (bound ledger) against the sorted path.
+
+The bound ledger runs multi-rotation lists through the hash-table step by
+default; TPGP_GB_HASH=0 selects the sorted per-rotation kernels.  Both must
+give bitwise the same keys, values, FIDs and ledgers (the bound ledger's
+fixed-point sums are order-independent), including maps whose keys span one
+to four words, maps that empty mid-step, steps that outgrow the table and
+the arena, and a cap hit mid-step.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from ddevol_gb300 import hamiltonians as H
+from ddevol_gb300.engine import Engine, GbLedger, options
+from gpu_helpers import bits, ledger_vec, random_map
+
+pytestmark = pytest.mark.gpu
+
+
+def evolve(hash_on, n, keys, vals, terms, dt, steps, opts, ledger=None):
+    os.environ["TPGP_GB_HASH"] = "1" if hash_on else "0"
+    try:
+        eng = Engine(0)
+        m = eng.map(n, keys, vals)
+        st, fids, led, msg = m.evolve(terms, dt, steps, opts, ledger or GbLedger())
+        k, v = m.download()
+        m.close()
+        eng.close()
+    finally:
+        os.environ.pop("TPGP_GB_HASH", None)
+    return st, k, v, fids, led, msg
+
+
+@pytest.mark.parametrize("n_spins", [24, 60, 90, 120])
+def test_hash_matches_sorted_random_maps(n_spins):
+    """Random multi-site maps (W = 1..4) under three steps of a ring with
+    next-nearest couplings: hash and sorted paths bitwise equal."""
+    rng = np.random.default_rng(n_spins)
+    keys, vals = random_map(rng, n_spins, 3000)
+    terms = H.ring_j1j2(n_spins, 1.0, 0.3)
+    opts = options(1e-4, exact_ledger=False)
+    a = evolve(True, n_spins, keys, vals, terms, 0.03, 3, opts)
+    b = evolve(False, n_spins, keys, vals, terms, 0.03, 3, opts)
+    assert a[0] == b[0] == 0, (a[5], b[5])
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(bits(a[2]), bits(b[2]))
+    assert np.array_equal(bits(a[3]), bits(b[3]))
+    assert np.array_equal(bits(ledger_vec(a[4])), bits(ledger_vec(b[4])))
+
+
+def test_map_that_empties_mid_step(oracle):
+    """A threshold above every value removes the whole map in the first
+    anticommuting rotation; the remaining rotations are no-ops (no ledger
+    change), as in the reference."""
+    terms = H.ring_j1j2(8)
+    k0, v0 = H.single_site_operator(8)
+    a = evolve(True, 8, k0, v0, terms, 0.05, 1, options(10.0, exact_ledger=False))
+    b = evolve(False, 8, k0, v0, terms, 0.05, 1, options(10.0, exact_ledger=False))
+    ost, ok, ov, oled = oracle.strang_step(k0, v0, 8, terms, 0.05, threshold=10.0, steps=1)
+    assert a[0] == b[0] == ost == 0
+    assert len(a[2]) == len(ov) == 0
+    assert a[4].rotations == b[4].rotations == oled.rotations
+    assert np.array_equal(bits(ledger_vec(a[4])), bits(ledger_vec(b[4])))
+
+
+def test_table_and_arena_growth_in_one_step(oracle):
+    """Eight spins, global X, threshold 0: the map grows from 8 terms to
+    thousands within a step, past the initial table and arena."""
+    terms = H.ring_j1j2(8)
+    k0, v0 = H.global_x_operator(8)
+    ost, ok, ov, _ = oracle.strang_step(k0, v0, 8, terms, 0.05, threshold=0.0, steps=3)
+    a = evolve(True, 8, k0, v0, terms, 0.05, 3, options(0.0, exact_ledger=False))
+    assert a[0] == ost == 0, a[5]
+    assert len(a[2]) > 4096
+    assert np.array_equal(a[1], ok) and np.array_equal(bits(a[2]), bits(ov))
+
+
+def test_cap_mid_step_is_transactional():
+    terms = H.ring_j1j2(16)
+    k0, v0 = H.single_site_operator(16)
+    base = evolve(True, 16, k0, v0, terms, 0.01, 20, options(1e-6, exact_ledger=False))
+    assert base[0] == 0
+    n20 = len(base[2])
+    a = evolve(True, 16, base[1], base[2], terms, 0.01, 1,
+               options(1e-6, max_terms=n20 + 3, exact_ledger=False))
+    b = evolve(False, 16, base[1], base[2], terms, 0.01, 1,
+               options(1e-6, max_terms=n20 + 3, exact_ledger=False))
+    assert a[0] == b[0] == 3  # ECAP
+    assert np.array_equal(a[1], base[1]) and np.array_equal(bits(a[2]), bits(base[2]))
