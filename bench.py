@@ -460,6 +460,7 @@ def run_powder(args, dist):
         batch.set_terms(k, terms, POWDER["dt"], opts)
     batch.step(args.warmup)
     clusters = batch.autotune()
+    tables = bool(batch.lib.tpgp_gb_batch_uses_tables(batch.ptr))
     sampler = ClockSampler(physical_gpu_index(dist.local_rank))
     sampler.start()
     time.sleep(0.3)
@@ -509,7 +510,8 @@ def run_powder(args, dist):
                    "items": len(items), "window_steps": [args.warmup, args.warmup + args.steps],
                    "terms_per_item_after": {"min": int(min(sizes)), "median": int(np.median(sizes)),
                                             "max": int(max(sizes))},
-                   "cluster_ctas_per_item": clusters, "failed_items": failed,
+                   "cluster_ctas_per_item": clusters, "cta_local_tables": tables,
+                   "failed_items": failed,
                    "ledger": "bound (fixed-point)",
                    "l2": "L2 flushed (512 MB write) between timed steps",
                    "parallelism": f"replicas x{dist.world}"},

@@ -83,12 +83,25 @@ __device__ __forceinline__ unsigned long long fmix64(unsigned long long h) {
     h ^= h >> 33;
     return h;
 }
+// Hash of a key: the words folded through the murmur3 64-bit finalizer.
+// (A plain multiplicative hash was tried: its low bits cluster on Pauli
+// keys, whose nonidentity sites are few, and probe chains grew ~20x.)
 template <int W>
 __device__ __forceinline__ unsigned long long hash_of(const Key<W>& k) {
     unsigned long long h = 0x9e3779b97f4a7c15ull;
 #pragma unroll
     for (int w = 0; w < W; ++w) h = fmix64(h ^ k.w[w]);
     return h;
+}
+
+// Branch data of key K and of its partner K xor Q from K's two site symbols
+// (the partner's symbols are K's xor (qi, qj)).
+__device__ __forceinline__ void pair_signs(const RotParams& p, uint64_t wi, uint64_t wj,
+                                           bool& anti, bool& plus_k, bool& plus_p) {
+    const unsigned pi = site_symbol(wi, p.i_shift), pj = site_symbol(wj, p.j_shift);
+    anti = anticommutes(p.qi, pi) != anticommutes(p.qj, pj);
+    plus_k = ((phase_exponent(p.qi, pi) + phase_exponent(p.qj, pj)) & 3u) == 1u;
+    plus_p = ((phase_exponent(p.qi, pi ^ p.qi) + phase_exponent(p.qj, pj ^ p.qj)) & 3u) == 1u;
 }
 
 // Slot of key k (tags other than `skip` compared), or -1 with *empty_at the
@@ -209,18 +222,13 @@ __device__ __forceinline__ unsigned long long settle(const RotParams& p, const K
     return out;
 }
 
-// Slots each thread carries through one loop iteration: their loads, and
-// then their first partner probes, are issued together so that several
-// global round trips are in flight per thread.
-template <int W>
-struct HashUnroll {
-    static constexpr int value = 1;
-};
-
-template <int W>
-__global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsigned r) {
-    constexpr int U = HashUnroll<W>::value;
-    __shared__ PairTally s_t[kHashBlock / 32];
+// One rotation over the table (one CTA's share of the slots): each slot's
+// tag, value and key are loaded in one round trip, and an anticommuting
+// key's first probe loads the probe slot's tag, key and value together.
+template <int W, int NT>
+__device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r) {
+    constexpr int U = 1;
+    __shared__ PairTally s_t[NT / 32];
     __shared__ unsigned long long s_acc[4];  // removed l1 (lo, hi), sq (lo, hi)
     if (threadIdx.x < 4) s_acc[threadIdx.x] = 0ull;
     __syncthreads();
@@ -357,7 +365,7 @@ __global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsig
     if (threadIdx.x == 0) {
         unsigned long long born = 0, died = 0, removed = 0, claimed = 0;
         unsigned flags = 0;
-        for (int w = 0; w < kHashBlock / 32; ++w) {
+        for (int w = 0; w < NT / 32; ++w) {
             born += s_t[w].born;
             died += s_t[w].died;
             removed += s_t[w].removed;
@@ -372,6 +380,23 @@ __global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsig
         if (removed) atomicAdd(&hs->removed, removed);
         if (claimed) atomicAdd(a.claimed, claimed);
         if (flags) atomicOr(&hs->flags, flags);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsigned r) {
+    hash_pass<W, kHashBlock>(a, r);
+}
+
+// All rotations of a step in one cooperative launch (one CTA of 1024 threads
+// per SM), a bounded grid barrier between rotations; a barrier that gives up
+// sets ST_TIMEOUT and the CTA leaves.  The passes are those of k_hash_rotate.
+constexpr int kHashPersistentBlock = 1024;
+template <int W>
+__global__ void __launch_bounds__(kHashPersistentBlock, 1) k_hash_rotate_all(HashArgs a) {
+    for (unsigned r = 0; r < a.rotations; ++r) {
+        hash_pass<W, kHashPersistentBlock>(a, r);
+        if (!grid_barrier(a.st)) return;
     }
 }
 
@@ -653,11 +678,16 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint64_t* sk
 // radix sort through the item's global scratch into its output buffer.  An
 // item whose table fills up reports ST_TABLE and is re-run on the clustered
 // sorted path.
-constexpr unsigned kSmemSlotsMax = 4096;
+// Per slot: tag, key, two values, and one entry of the occupied-slot list.
 template <int W>
 constexpr size_t smem_slot_bytes() {
-    return 4 + 8 * W + 16;
+    return 4 + 8 * W + 16 + 4;
 }
+template <int W>
+constexpr unsigned smem_slots_max() {
+    return W <= 3 ? 4096u : 2048u;  // tables up to ~200 KB of shared memory
+}
+constexpr unsigned kSmemSlotsMax = 4096;
 
 template <int W>
 __device__ __forceinline__ long long smem_find(const uint32_t* tags, const uint64_t* keys,
@@ -715,6 +745,8 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
     sv[0] = reinterpret_cast<unsigned long long*>(skeys + (size_t)S * W);
     sv[1] = sv[0] + S;
     uint32_t* stags = reinterpret_cast<uint32_t*>(sv[1] + S);
+    unsigned* socc = stags + S;  // occupied slots, in claim order
+    __shared__ unsigned s_nocc, s_nocc0;  // count; count when the rotation started
     DeviceState* st = it.scratch.st;
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     for (unsigned k = tid; k < S; k += blockDim.x) {
@@ -724,7 +756,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
     }
     if (tid < 4) s_acc[tid] = 0ull;
     if (tid == 0) {
-        s_born = s_died = s_removed = s_flags = 0u;
+        s_born = s_died = s_removed = s_flags = s_nocc = 0u;
         s_status = st->status;
         s_n = st->n;
     }
@@ -738,10 +770,15 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
             const Key<W> key = load_key<W>(in_k, k);
             const long long slot =
                 smem_insert<W>(stags, skeys, mask, key, (unsigned)hash_of<W>(key) & mask, 1u, &overflow);
-            if (slot >= 0) sv[0][slot] = dbits(__ldcg(in_v + k));
+            if (slot >= 0) {
+                sv[0][slot] = dbits(__ldcg(in_v + k));
+                socc[atomicAdd(&s_nocc, 1u)] = (unsigned)slot;
+            }
         }
         if (overflow) atomicOr(&s_flags, ST_TABLE);
     }
+    __syncthreads();
+    if (tid == 0) s_nocc0 = s_nocc;
     __syncthreads();
     Ledger led;
     unsigned long long terms = 0;
@@ -757,15 +794,18 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
         PairTally t;
         t.born = t.died = t.removed = t.claimed = 0;
         t.flags = 0;
-        for (unsigned slot = tid; slot < S; slot += blockDim.x) {
-            const uint32_t tag = stags[slot];
-            if (tag == 0u || tag >= stamp) continue;
+        // one pass over the occupied slots present when the rotation starts
+        // (keys it inserts are appended behind them)
+        const int top = p.mbit[0];
+        const unsigned nocc = s_nocc0;
+        for (unsigned k = tid; k < nocc; k += blockDim.x) {
+            const unsigned slot = socc[k];
             const unsigned long long vb = vin[slot];
             Key<W> K;
 #pragma unroll
             for (int w = 0; w < W; ++w) K.w[w] = skeys[(size_t)slot * W + w];
-            bool anti, plus_k;
-            branch_info(p, word_at<W>(K, p.i_word), word_at<W>(K, p.j_word), anti, plus_k);
+            bool anti, plus_k, plus_p;
+            pair_signs(p, word_at<W>(K, p.i_word), word_at<W>(K, p.j_word), anti, plus_k, plus_p);
             if (!anti) {
                 vout[slot] = vb ? settle<W>(p, K, from_bits(vb), true, t, s_acc) : 0ull;
                 continue;
@@ -784,9 +824,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
                 if (!p_live) vout[slot] = 0ull;
                 continue;
             }
-            if (p_live && key_less<W>(P, K)) continue;
-            bool anti_p, plus_p;
-            branch_info(p, word_at<W>(P, p.i_word), word_at<W>(P, p.j_word), anti_p, plus_p);
+            if (p_live && key_bit<W>(K, top)) continue;
             const double v = from_bits(vb);
             double sk = __dmul_rn(v, s);
             if (!plus_k) sk = negate(sk);
@@ -804,8 +842,12 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
                 vout[ps] = pbits;
             } else if (pbits) {
                 const long long ns = smem_insert<W>(stags, skeys, mask, P, empty_at, stamp, &overflow);
-                if (ns >= 0) vout[ns] = pbits;
-                else t.flags |= ST_TABLE;
+                if (ns >= 0) {
+                    vout[ns] = pbits;
+                    socc[atomicAdd(&s_nocc, 1u)] = (unsigned)ns;
+                } else {
+                    t.flags |= ST_TABLE;
+                }
             }
         }
 #pragma unroll
@@ -861,6 +903,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
             s_status = status;
             s_acc[0] = s_acc[1] = s_acc[2] = s_acc[3] = 0ull;
             s_born = s_died = s_removed = 0u;
+            s_nocc0 = s_nocc;  // this rotation's insertions are done (barrier above)
         }
         __syncthreads();
     }
@@ -876,8 +919,10 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
     const unsigned long long* vf = sv[it.rotations & 1u];
     if (tid == 0) s_count = 0u;
     __syncthreads();
-    for (unsigned slot = tid; slot < S; slot += blockDim.x) {
-        const bool live = stags[slot] != 0u && vf[slot] != 0ull;
+    const unsigned nocc_end = (s_nocc + 31u) & ~31u;  // whole warps for the ballot
+    for (unsigned k = tid; k < nocc_end; k += blockDim.x) {
+        const unsigned slot = k < s_nocc ? socc[k] : 0u;
+        const bool live = k < s_nocc && vf[slot] != 0ull;
         const unsigned m = __ballot_sync(0xffffffffu, live);
         unsigned at = 0;
         if (lane == 0 && m) at = atomicAdd(&s_count, (unsigned)__popc(m));

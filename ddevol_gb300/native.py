@@ -139,6 +139,8 @@ def _bind(lib):
     lib.tpgp_gb_batch_cluster.argtypes = [C.c_void_p, sz]
     lib.tpgp_gb_batch_set_cluster.restype = C.c_int
     lib.tpgp_gb_batch_set_cluster.argtypes = [C.c_void_p, sz, C.c_int, sz, charp, sz]
+    lib.tpgp_gb_batch_uses_tables.restype = C.c_int
+    lib.tpgp_gb_batch_uses_tables.argtypes = [C.c_void_p]
     lib.tpgp_gb_batch_max_cluster.restype = C.c_int
     lib.tpgp_gb_batch_max_cluster.argtypes = [C.c_void_p, sz]
     lib.tpgp_gb_batch_item_status.restype = C.c_int

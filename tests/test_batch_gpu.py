@@ -6,6 +6,8 @@ item's keys, values, per-step FID and ledger must equal those of
 tpgp_gb_strang_step on that item alone, for every cluster size the
 autotuner may pick.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -31,8 +33,21 @@ def bits(a):
     return np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
 
 
+@pytest.fixture
+def smem_off():
+    """Batches created inside run every item on the clustered sorted path."""
+    os.environ["TPGP_GB_BATCH_SMEM"] = "0"
+    yield
+    os.environ.pop("TPGP_GB_BATCH_SMEM", None)
+
+
+@pytest.mark.parametrize("path", ["auto", "clustered"])
 @pytest.mark.parametrize("exact", [False, True])
-def test_batch_matches_single_solves(engine, exact):
+def test_batch_matches_single_solves(engine, exact, path, request):
+    """Bound-ledger items run in CTA-local hash tables (auto), or all items on
+    the clustered sorted path; exact-ledger items always take the latter."""
+    if path == "clustered":
+        request.getfixturevalue("smem_off")
     items = powder_items(12)
     steps, dt = 6, 0.02
     batch = Batch(engine, [n for n, _, _ in items])
@@ -57,7 +72,7 @@ def test_batch_matches_single_solves(engine, exact):
 
 
 @pytest.mark.parametrize("shape", ["autotune", (1, 0), (2, 0), (4, 64), (8, 32), (1, 16)])
-def test_batch_cluster_sizes_agree(engine, shape):
+def test_batch_cluster_sizes_agree(engine, shape, smem_off):
     """Every cluster shape gives the single-solve result: autotuned base
     sizes, forced base sizes, and small terms-per-CTA so that the size rule
     puts the larger items on 8- and 16-CTA clusters."""
@@ -104,4 +119,36 @@ def test_batch_item_failure_is_isolated(engine):
     assert len(v1) == 1  # still the initial operator
     for k in (0, 2, 3):
         assert batch.item_status(k) == 0 and batch.item_len(k) > 1
+    batch.close()
+
+
+def test_cta_table_overflow_falls_back(engine):
+    """Items that outgrow their CTA-local table within a step (global X on
+    eight spins, threshold 0: 8 terms to thousands) are re-run on the
+    clustered path; results equal the single-map solve."""
+    n, dt, steps = 8, 0.05, 3
+    terms = H.ring_j1j2(n)
+    batch = Batch(engine, [n, n, 20])
+    k8, v8 = H.global_x_operator(n)
+    batch.upload(0, k8, v8)
+    batch.set_terms(0, terms, dt, options(0.0, exact_ledger=False))
+    batch.upload(1, k8, v8)
+    batch.set_terms(1, terms, dt, options(1e-3, exact_ledger=False))
+    k20, v20 = H.single_site_operator(20, 0)
+    batch.upload(2, k20, v20)
+    batch.set_terms(2, H.ring_j1j2(20), dt, options(1e-5, exact_ledger=False))
+    fids = batch.step(steps)
+    for item, (nn, kk, vv, tt, thr) in enumerate([(n, k8, v8, terms, 0.0), (n, k8, v8, terms, 1e-3),
+                                                   (20, k20, v20, H.ring_j1j2(20), 1e-5)]):
+        assert batch.item_status(item) == 0
+        m = engine.map(nn, kk, vv)
+        st, f1, led1, msg = m.evolve(tt, dt, steps, options(thr, exact_ledger=False))
+        assert st == 0, msg
+        k1, v1 = m.download()
+        m.close()
+        k2, v2 = batch.download(item)
+        assert np.array_equal(k1, k2) and np.array_equal(bits(v1), bits(v2)), item
+        assert np.array_equal(bits(f1), bits(fids[:, item])), item
+        assert led1.as_dict() == batch.ledger(item).as_dict(), item
+    assert batch.item_len(0) > 4096
     batch.close()

@@ -89,3 +89,33 @@ def test_cap_mid_step_is_transactional():
                options(1e-6, max_terms=n20 + 3, exact_ledger=False))
     assert a[0] == b[0] == 3  # ECAP
     assert np.array_equal(a[1], base[1]) and np.array_equal(bits(a[2]), bits(base[2]))
+
+
+def test_persistent_hash_step(golden_trajectories):
+    """TPGP_GB_HASH_PERSISTENT=1 runs a step's rotations in one cooperative
+    launch with grid barriers: same results as the per-rotation launches."""
+    g = golden_trajectories
+    p = "ring16__"
+    terms = [(int(a), int(b), int(c), int(d), float(h))
+             for (a, b, c, d), h in zip(g[p + "terms"], g[p + "h"])]
+    opts = options(float(g[p + "threshold"]), exact_ledger=False)
+    args = (int(g[p + "n"]), g[p + "in_keys"], g[p + "in_values"], terms, float(g[p + "dt"]),
+            int(g[p + "steps"]), opts)
+    os.environ["TPGP_GB_HASH_PERSISTENT"] = "1"
+    try:
+        a = evolve(True, *args)
+        rng = np.random.default_rng(60)
+        keys, vals = random_map(rng, 60, 3000)
+        ra = evolve(True, 60, keys, vals, H.ring_j1j2(60, 1.0, 0.3), 0.03, 2,
+                    options(1e-4, exact_ledger=False))
+    finally:
+        os.environ.pop("TPGP_GB_HASH_PERSISTENT", None)
+    assert a[0] == 0, a[5]
+    assert np.array_equal(a[1], g[p + "out_keys"])
+    assert np.array_equal(bits(a[2]), bits(g[p + "out_values"]))
+    assert np.array_equal(bits(a[3]), bits(g[p + "fid_sum"]))
+    rb = evolve(False, 60, keys, vals, H.ring_j1j2(60, 1.0, 0.3), 0.03, 2,
+                options(1e-4, exact_ledger=False))
+    assert ra[0] == rb[0] == 0
+    assert np.array_equal(ra[1], rb[1]) and np.array_equal(bits(ra[2]), bits(rb[2]))
+    assert np.array_equal(bits(ledger_vec(ra[4])), bits(ledger_vec(rb[4])))

@@ -5,7 +5,7 @@
   cubic, 96-site chain): final keys, values and ledger bitwise, the per-step
   FID sum (tpgp_map_single_sum) bitwise, the per-step term count;
 * graph replay and plain launches give identical results;
-* the fast (tree) ledger keeps keys/values bitwise and stays within its bound;
+* the bound (fixed-point) ledger keeps keys/values bitwise and stays within its bound;
 * transactional failures: a cap or budget hit mid-step, an invalid term after
   valid ones, leave map and ledger untouched.
 """
