@@ -266,14 +266,14 @@ def algorithmic_bytes(words, n_in_sum, n_out_sum):
     return (8 * words + 8) * (n_in_sum + n_out_sum)
 
 
-def read_traffic_profile(kernel, cfg_name):
-    """Per-input-term DRAM bytes of `kernel` from the committed ncu summary
-    (profiles/<kernel>_<config>.md, line 'dram_bytes_per_input_term: X')."""
+def read_traffic_profile(kernel, cfg_name, key="dram_bytes_per_input_term"):
+    """Per-input-term bytes of `kernel` from the committed ncu summary
+    (profiles/<kernel>_<config>.md, line '<key>: X'; DRAM by default)."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{cfg_name}.md")
     try:
         with open(path) as f:
             for line in f:
-                if line.strip().startswith("dram_bytes_per_input_term:"):
+                if line.strip().startswith(key + ":"):
                     return float(line.split(":", 1)[1])
     except OSError:
         return None
@@ -343,6 +343,8 @@ def run_gb300(args, dist):
     path_achieved = algorithmic_bytes(words, n_in_sum, n_out_sum) / (total_ms / 1e3) / 1e9
     traffic_per_term = read_traffic_profile(dominant, args.config)
     traffic = None if traffic_per_term is None else traffic_per_term * (n_in_sum / rot)
+    l2_per_term = read_traffic_profile(dominant, args.config, "l2_bytes_per_input_term")
+    l2_traffic = None if l2_per_term is None else l2_per_term * (n_in_sum / rot)
 
     # ---- end to end through the C-ABI with pinned host buffers
     e2e = None
@@ -422,6 +424,7 @@ def run_gb300(args, dist):
         "roofline": {
             "bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "l2_traffic": l2_traffic,
             "bytes_per_launch": bytes_per_launch, "launch_ms": dom_ms / dom_n,
             "kernel_share": dom_ms / total_ms,
             "path_achieved": path_achieved, "path_frac": path_achieved / peak,
