@@ -13,7 +13,7 @@ K steps are timed.
 Metric: Pauli terms/s = (sum over the timed rotations of the rotation's input
 terms) / device time of the K steps (CUDA events on the engine's stream).
 
-Extra keys (see DESIGN.md): e2e (same metric through the C-ABI with host
+Extra keys: e2e (same metric through the C-ABI with host
 buffers: every step uploads the map from pinned host memory, runs the step
 and downloads the result), roofline (HBM bound, the dominant kernel's
 algorithmic bytes per launch over its average launch time, from a profiled
@@ -358,7 +358,7 @@ def run_gb300(args, dist):
         hv[:len(v)] = v
         n_host = len(v)
         e2e_terms, e2e_s, h2d, d2h = 0, 0.0, 0, 0
-        e2e_steps = max(1, min(args.steps, 2))
+        e2e_steps = max(1, args.steps)
         dist.barrier()
         for _ in range(e2e_steps):
             t0 = time.perf_counter()

@@ -59,7 +59,7 @@ struct HashArgs {
     uint32_t* tags;
     uint64_t* keys;                 // [S][W]
     unsigned long long* vals[2];    // coefficient bit patterns, double-buffered
-    unsigned long long mask;        // S - 1 (S a power of two)
+    unsigned long long slots;       // S (any size: slots are h * S >> 64)
     HashStat* stats;                // [rotations][kStatSlots]
     unsigned long long* claimed;    // slots claimed during the step
     const uint64_t* in_keys;        // the step's input map (never written); its
@@ -94,6 +94,15 @@ __device__ __forceinline__ unsigned long long hash_of(const Key<W>& k) {
     return h;
 }
 
+// Table slot of a hash (the high word of h * S: uniform over any S) and the
+// next slot of a linear probe.
+__device__ __forceinline__ unsigned long long slot_of(unsigned long long h, unsigned long long S) {
+    return __umul64hi(h, S);
+}
+__device__ __forceinline__ unsigned long long next_slot(unsigned long long s, unsigned long long S) {
+    return s + 1 == S ? 0ull : s + 1;
+}
+
 // Branch data of key K and of its partner K xor Q from K's two site symbols
 // (the partner's symbols are K's xor (qi, qj)).
 __device__ __forceinline__ void pair_signs(const RotParams& p, uint64_t wi, uint64_t wj,
@@ -109,7 +118,7 @@ __device__ __forceinline__ void pair_signs(const RotParams& p, uint64_t wi, uint
 template <int W>
 __device__ __forceinline__ long long hash_find(const HashArgs& a, const Key<W>& k, uint32_t skip,
                                                unsigned long long* empty_at, bool* overflow) {
-    unsigned long long s = hash_of<W>(k) & a.mask;
+    unsigned long long s = slot_of(hash_of<W>(k), a.slots);
     for (int i = 0; i < kMaxProbe; ++i) {
         const uint32_t tag = __ldcg(a.tags + s);
         if (tag == 0) {
@@ -117,7 +126,7 @@ __device__ __forceinline__ long long hash_find(const HashArgs& a, const Key<W>& 
             return -1;
         }
         if (tag != skip && key_eq<W>(load_key<W>(a.keys, s), k)) return (long long)s;
-        s = (s + 1) & a.mask;
+        s = next_slot(s, a.slots);
     }
     *overflow = true;
     return -1;
@@ -134,7 +143,7 @@ __device__ __forceinline__ long long hash_insert(const HashArgs& a, const Key<W>
             store_key<W>(a.keys, s, k);
             return (long long)s;
         }
-        s = (s + 1) & a.mask;
+        s = next_slot(s, a.slots);
     }
     *overflow = true;
     return -1;
@@ -168,7 +177,7 @@ __global__ void __launch_bounds__(kHashBlock) k_hash_build(HashArgs a) {
     for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += stride) {
         const Key<W> key = load_key<W>(a.in_keys, k);
-        const long long s = hash_insert<W>(a, key, hash_of<W>(key) & a.mask, 1u, &overflow);
+        const long long s = hash_insert<W>(a, key, slot_of(hash_of<W>(key), a.slots), 1u, &overflow);
         if (s >= 0) {
             a.vals[0][s] = dbits(__ldcg(a.in_vals + k));
             ++claimed;
@@ -241,7 +250,7 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r) {
     PairTally t;
     t.born = t.died = t.removed = t.claimed = 0;
     t.flags = 0;
-    const unsigned long long S = a.mask + 1;
+    const unsigned long long S = a.slots;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
          base < S; base += U * stride) {
@@ -281,7 +290,7 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r) {
             }
             act[u] = true;
             P[u] = key_xor<W>(K[u], Q);
-            ps[u] = hash_of<W>(P[u]) & a.mask;
+            ps[u] = slot_of(hash_of<W>(P[u]), a.slots);
             pt[u] = __ldcg(a.tags + ps[u]);
             PK[u] = load_key<W>(a.keys, ps[u]);
             pv[u] = __ldcg(vin + ps[u]);
@@ -306,7 +315,7 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r) {
                     overflow = false;
                     break;
                 }
-                ps[u] = (ps[u] + 1) & a.mask;
+                ps[u] = next_slot(ps[u], a.slots);
                 pt[u] = __ldcg(a.tags + ps[u]);
                 PK[u] = load_key<W>(a.keys, ps[u]);
                 pv[u] = __ldcg(vin + ps[u]);
@@ -536,7 +545,7 @@ template <int W>
 __global__ void __launch_bounds__(kHashBlock) k_hash_extract(HashArgs a) {
     if (__ldcg(&a.st->status)) return;
     const unsigned long long* vf = a.vals[a.rotations & 1u];
-    const unsigned long long S = a.mask + 1;
+    const unsigned long long S = a.slots;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     // every lane runs the same trip count so the warp ballots stay converged
@@ -575,7 +584,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_hist(const uint64_t* keys,
                                                            int d) {
     __shared__ unsigned cnt[256];
     if (__ldcg(&a.st->status)) return;
-    const unsigned long long n = min(__ldcg(&a.st->n), a.mask + 1);  // never beyond the buffers
+    const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
     if (d == 0 && blockIdx.x == 0 && threadIdx.x == 0 && __ldcg(&a.st->n_out) != n)
         atomicOr(&a.st->status, ST_ORDER);  // extraction must find exactly the committed count
     const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
@@ -597,7 +606,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_hist(const uint64_t* keys,
 __global__ void __launch_bounds__(1024) k_radix_scan(HashArgs a) {
     __shared__ unsigned long long s_part[1024];
     if (__ldcg(&a.st->status)) return;
-    const unsigned long long n = min(__ldcg(&a.st->n), a.mask + 1);  // never beyond the buffers
+    const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
     const unsigned long long total = 256ull * ((n + kSortTile - 1) / kSortTile);
     const unsigned long long per = (total + blockDim.x - 1) / blockDim.x;
     const unsigned long long lo = min(total, per * threadIdx.x), hi = min(total, lo + per);
@@ -629,7 +638,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint64_t* sk
     __shared__ unsigned base[256];
     __shared__ unsigned wcnt[kSortBlock / 32][256];
     if (__ldcg(&a.st->status)) return;
-    const unsigned long long n = min(__ldcg(&a.st->n), a.mask + 1);  // never beyond the buffers
+    const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
     const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {

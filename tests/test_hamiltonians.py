@@ -9,7 +9,7 @@ from ddevol_gb300 import hamiltonians as H
 def test_ring16_j1j2_terms():
     terms = H.ring_j1j2(16)
     assert len(terms) == 96
-    # BASELINE's /2 convention through the reference edge with d' = 2d
+    # the configurations' d (2ZZ - XX - YY) / 2 convention, passed to the reference edge as d' = 2d
     assert terms[0] == (0, 1, 3, 3, 1.0)
     assert terms[1] == (0, 1, 1, 1, -0.5)
     assert terms[3] == (0, 2, 3, 3, 0.125)
