@@ -160,7 +160,12 @@ def physical_gpu_index(local_rank):
 
 # ------------------------------------------------------------ distributed
 class Dist:
-    def __init__(self):
+    """Ranks of a multi-GPU run (torchrun env).  Replicas only: the process
+    group carries the barrier around the timed region and the max / sum of
+    the per-rank results, never solve data.  backend: "nccl" (GPUs) or
+    "gloo" (host; the CPU tests of this class)."""
+
+    def __init__(self, backend=None):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -168,8 +173,11 @@ class Dist:
         if self.world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(self.local_rank)
-            dist.init_process_group("nccl")
+            backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend)
+            self.device = "cuda" if backend == "nccl" else "cpu"
             self.dist = dist
             self.torch = torch
             self.pg = True
@@ -181,7 +189,7 @@ class Dist:
     def reduce(self, value, op="max"):
         if not self.pg:
             return value
-        t = self.torch.tensor([float(value)], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([float(value)], dtype=self.torch.float64, device=self.device)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
         return float(t.item())
 
@@ -455,7 +463,7 @@ def run_powder(args, dist):
     clustered launch (per key width) replayed from a CUDA graph."""
     from ddevol_gb300.engine import Batch, Engine, options
     eng = Engine(dist.local_rank)
-    items = powder_items()
+    items = powder_items(seed=POWDER["seed"] + 7919 * dist.rank)  # each replica its own orientations
     batch = Batch(eng, [n for n, _ in items])
     opts = options(POWDER["threshold"], exact_ledger=False)
     for k, (n, terms) in enumerate(items):
