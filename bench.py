@@ -659,8 +659,10 @@ def run_reference(args, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (trajectory generated from X_0; no dataset)",
         "config": {"workload": f"{args.config}_trajectory_window", "description": cfg["label"],
-                   "n_spins": cfg["n"], "key_words": words, "setup_steps": setup_steps,
-                   "terms_at_window_start": len(v), "parallelism": "host cores"},
+                   "n_spins": cfg["n"], "key_words": words, "hamiltonian_terms": len(terms),
+                   "rotations_per_step": 2 * len(terms), "setup_steps": setup_steps,
+                   "terms_at_window_start": len(v), "ledger": "exact (sequential)",
+                   "parallelism": "host cores"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
