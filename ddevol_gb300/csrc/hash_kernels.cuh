@@ -56,6 +56,8 @@ static_assert(sizeof(HashStat) == 64, "stat slot is one 64-byte line");
 struct HashArgs {
     const RotParams* ps;  // the step's rotation list (device)
     unsigned rotations;
+    const uint2* runs;    // fused passes: (first rotation, count) per pass
+    unsigned passes;      // kernels over the table (= rotations when not fused)
     uint32_t* tags;
     uint64_t* keys;                 // [S][W]
     unsigned long long* vals[2];    // coefficient bit patterns, double-buffered
@@ -235,16 +237,16 @@ __device__ __forceinline__ unsigned long long settle(const RotParams& p, const K
 // tag, value and key are loaded in one round trip, and an anticommuting
 // key's first probe loads the probe slot's tag, key and value together.
 template <int W, int NT>
-__device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r) {
+__device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r, unsigned k) {
     constexpr int U = 1;
     __shared__ PairTally s_t[NT / 32];
     __shared__ unsigned long long s_acc[4];  // removed l1 (lo, hi), sq (lo, hi)
     if (threadIdx.x < 4) s_acc[threadIdx.x] = 0ull;
     __syncthreads();
     const RotParams& p = a.ps[r];
-    const uint32_t stamp = r + 2u;
-    const unsigned long long* vin = a.vals[r & 1u];
-    unsigned long long* vout = a.vals[(r + 1u) & 1u];
+    const uint32_t stamp = k + 2u;  // pass k: stamps and buffers; rotation r: parameters
+    const unsigned long long* vin = a.vals[k & 1u];
+    unsigned long long* vout = a.vals[(k + 1u) & 1u];
     const Key<W> Q = mask_key<W>(p);
     const double c = p.c, s = p.s;
     PairTally t;
@@ -393,8 +395,8 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r) {
 }
 
 template <int W>
-__global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsigned r) {
-    hash_pass<W, kHashBlock>(a, r);
+__global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsigned r, unsigned k) {
+    hash_pass<W, kHashBlock>(a, r, k);
 }
 
 // All rotations of a step in one cooperative launch (one CTA of 1024 threads
@@ -404,8 +406,216 @@ constexpr int kHashPersistentBlock = 1024;
 template <int W>
 __global__ void __launch_bounds__(kHashPersistentBlock, 1) k_hash_rotate_all(HashArgs a) {
     for (unsigned r = 0; r < a.rotations; ++r) {
-        hash_pass<W, kHashPersistentBlock>(a, r);
+        hash_pass<W, kHashPersistentBlock>(a, r, r);
         if (!grid_barrier(a.st)) return;
+    }
+}
+
+// ------------------------------------------------- fused runs on one site pair
+// A run of consecutive rotations on the same two sites (a secular edge's ZZ,
+// XX, YY; six at the middle of a Strang step) whose generators span a group
+// G of at most four XOR patterns G = {0, b1, b2, b1 ^ b2}.  Every key's coset
+// K xor G is closed under each rotation of the run, so each coset is evolved
+// on its own through the whole run — per rotation exactly the pair rule of
+// hash_pass (commuting members keep v + 0, anticommuting members combine
+// with their partner a ^ label(Q)), with the zero drop, threshold and
+// removed-weight sums of that rotation — and only the final values are
+// written.  The smallest live member's thread evolves a coset; a coset with
+// no live member has each member's own thread clear its slot.  Results are
+// those of the run's rotations one by one.
+constexpr int kMaxRun = 6;
+
+template <int W>
+__device__ __forceinline__ void coset_sign(const RotParams& p, const Key<W>& m, bool& anti,
+                                           bool& plus) {
+    branch_info(p, word_at<W>(m, p.i_word), word_at<W>(m, p.j_word), anti, plus);
+}
+
+template <int W>
+__global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned k) {
+    __shared__ unsigned long long s_acc[kMaxRun][4];
+    __shared__ unsigned s_cnt[kMaxRun][3];  // born, died, removed
+    __shared__ unsigned s_claimed, s_flags;
+    for (int q = threadIdx.x; q < kMaxRun * 4; q += blockDim.x) (&s_acc[0][0])[q] = 0ull;
+    for (int q = threadIdx.x; q < kMaxRun * 3; q += blockDim.x) (&s_cnt[0][0])[q] = 0u;
+    if (threadIdx.x == 0) {
+        s_claimed = 0u;
+        s_flags = 0u;
+    }
+    __syncthreads();
+    const uint2 run = a.runs[k];
+    const unsigned r0 = run.x, L = run.y;
+    const uint32_t stamp = k + 2u;
+    const unsigned long long* vin = a.vals[k & 1u];
+    unsigned long long* vout = a.vals[(k + 1u) & 1u];
+    // the run's group: G[1] = the first mask, G[2] the first other mask
+    Key<W> G[4];
+#pragma unroll
+    for (int w = 0; w < W; ++w) G[0].w[w] = 0ull;
+    G[1] = mask_key<W>(a.ps[r0]);
+    G[2] = G[0];
+    bool has_b2 = false;
+    for (unsigned l = 1; l < L; ++l) {
+        const Key<W> q = mask_key<W>(a.ps[r0 + l]);
+        if (!has_b2 && !key_eq<W>(q, G[1])) {
+            G[2] = q;
+            has_b2 = true;
+        }
+    }
+    G[3] = key_xor<W>(G[1], G[2]);
+    const int gs = has_b2 ? 4 : 2;
+    unsigned flags = 0u, claimed = 0u;
+    const unsigned long long S = a.slots;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long slot = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+         slot < S; slot += stride) {
+        const uint32_t tag = __ldcg(a.tags + slot);
+        const unsigned long long vb = __ldcg(vin + slot);
+        const Key<W> K = load_key<W>(a.keys, slot);
+        if (tag == 0u || tag >= stamp) continue;  // empty, or inserted by this pass
+        // the coset's other members: first probe slots loaded together
+        Key<W> M[4], PK[4];
+        unsigned long long ps[4], pv[4], ea[4], v[4];
+        uint32_t pt[4];
+        long long sl[4];
+        M[0] = K;
+        sl[0] = (long long)slot;
+        v[0] = vb;
+        ea[0] = 0ull;
+#pragma unroll
+        for (int m = 1; m < 4; ++m) {
+            M[m] = key_xor<W>(K, G[m]);
+            sl[m] = -1;
+            v[m] = 0ull;
+            ea[m] = 0ull;
+            if (m < gs) {
+                ps[m] = slot_of(hash_of<W>(M[m]), S);
+                pt[m] = __ldcg(a.tags + ps[m]);
+                PK[m] = load_key<W>(a.keys, ps[m]);
+                pv[m] = __ldcg(vin + ps[m]);
+            }
+        }
+        bool overflow = false;
+#pragma unroll
+        for (int m = 1; m < 4; ++m) {
+            if (m >= gs) continue;
+            bool done = false;
+            for (int i = 0; i < kMaxProbe; ++i) {
+                if (pt[m] == 0u) {
+                    ea[m] = ps[m];
+                    done = true;
+                    break;
+                }
+                if (pt[m] != stamp && key_eq<W>(PK[m], M[m])) {
+                    sl[m] = (long long)ps[m];
+                    v[m] = pv[m];
+                    done = true;
+                    break;
+                }
+                ps[m] = next_slot(ps[m], S);
+                pt[m] = __ldcg(a.tags + ps[m]);
+                PK[m] = load_key<W>(a.keys, ps[m]);
+                pv[m] = __ldcg(vin + ps[m]);
+            }
+            if (!done) overflow = true;
+        }
+        if (overflow) {
+            flags |= ST_TABLE;
+            continue;
+        }
+        // the smallest live member evolves the coset
+        int h = -1;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+            if (m < gs && v[m] && (h < 0 || key_less<W>(M[m], pick<4, Key<W>>(M, h)))) h = m;
+        if (h < 0) {
+            vout[slot] = 0ull;  // no live member: each member clears its own slot
+            continue;
+        }
+        if (h != 0) continue;
+        double x[4];
+        bool live[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            live[m] = v[m] != 0ull;
+            x[m] = from_bits(v[m]);
+        }
+        for (unsigned l = 0; l < L; ++l) {
+            const RotParams& p = a.ps[r0 + l];
+            const Key<W> q = mask_key<W>(p);
+            const int b = key_eq<W>(q, G[1]) ? 1 : (key_eq<W>(q, G[2]) ? 2 : 3);
+            const double c = p.c, s = p.s;
+            bool anti[4], plus[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) coset_sign<W>(p, M[m], anti[m], plus[m]);
+            double nx[4];
+            bool touched[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                nx[m] = 0.0;
+                touched[m] = false;
+                if (m >= gs) continue;
+                if (!anti[m]) {
+                    nx[m] = x[m];
+                    touched[m] = live[m];
+                    continue;
+                }
+                const int pb = m ^ b;
+                const bool lp = pick<4, bool>(live, pb);
+                double sp = __dmul_rn(pick<4, double>(x, pb), s);  // partner's sin child
+                if (!pick<4, bool>(plus, pb)) sp = negate(sp);
+                if (live[m] && lp) nx[m] = __dadd_rn(__dmul_rn(x[m], c), sp);
+                else if (live[m]) nx[m] = __dmul_rn(x[m], c);
+                else if (lp) nx[m] = sp;
+                touched[m] = live[m] || lp;
+            }
+            PairTally t;
+            t.born = t.died = t.removed = t.claimed = 0u;
+            t.flags = 0u;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (!touched[m]) continue;  // absent before and after: no term
+                const unsigned long long out = settle<W>(p, M[m], nx[m], live[m], t, s_acc[l]);
+                live[m] = out != 0ull;
+                x[m] = from_bits(out);
+            }
+            if (t.born) atomicAdd(&s_cnt[l][0], t.born);
+            if (t.died) atomicAdd(&s_cnt[l][1], t.died);
+            if (t.removed) atomicAdd(&s_cnt[l][2], t.removed);
+            flags |= t.flags;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            if (m >= gs) continue;
+            const unsigned long long bits = live[m] ? dbits(x[m]) : 0ull;
+            if (sl[m] >= 0) {
+                vout[sl[m]] = bits;
+            } else if (bits) {
+                bool ovf = false;
+                const long long ns = hash_insert<W>(a, M[m], ea[m], stamp, &ovf);
+                if (ns >= 0) {
+                    vout[ns] = bits;
+                    ++claimed;
+                } else {
+                    flags |= ST_TABLE;
+                }
+            }
+        }
+    }
+    if (flags) atomicOr(&s_flags, flags);
+    if (claimed) atomicAdd(&s_claimed, claimed);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned l = 0; l < L; ++l) {
+            HashStat* hs = a.stats + (size_t)(r0 + l) * kStatSlots + (blockIdx.x % kStatSlots);
+            atomic_add_u128(&hs->l1_lo, &hs->l1_hi, U128{s_acc[l][0], s_acc[l][1]});
+            atomic_add_u128(&hs->sq_lo, &hs->sq_hi, U128{s_acc[l][2], s_acc[l][3]});
+            if (s_cnt[l][0]) atomicAdd(&hs->born, (unsigned long long)s_cnt[l][0]);
+            if (s_cnt[l][1]) atomicAdd(&hs->died, (unsigned long long)s_cnt[l][1]);
+            if (s_cnt[l][2]) atomicAdd(&hs->removed, (unsigned long long)s_cnt[l][2]);
+            if (s_flags) atomicOr(&hs->flags, s_flags);
+        }
+        if (s_claimed) atomicAdd(a.claimed, (unsigned long long)s_claimed);
     }
 }
 
@@ -544,7 +754,7 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
 template <int W>
 __global__ void __launch_bounds__(kHashBlock) k_hash_extract(HashArgs a) {
     if (__ldcg(&a.st->status)) return;
-    const unsigned long long* vf = a.vals[a.rotations & 1u];
+    const unsigned long long* vf = a.vals[a.passes & 1u];
     const unsigned long long S = a.slots;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;

@@ -119,3 +119,24 @@ def test_persistent_hash_step(golden_trajectories):
     assert ra[0] == rb[0] == 0
     assert np.array_equal(ra[1], rb[1]) and np.array_equal(bits(ra[2]), bits(rb[2]))
     assert np.array_equal(bits(ledger_vec(ra[4])), bits(ledger_vec(rb[4])))
+
+
+def test_fused_runs_match():
+    """TPGP_GB_HASH_FUSE=1: one pass per run of rotations on a site pair
+    (each coset evolved through the run) instead of one pass per rotation;
+    same maps, FIDs and ledgers."""
+    rng = np.random.default_rng(42)
+    keys, vals = random_map(rng, 40, 3000)
+    terms = H.ring_j1j2(40, 1.0, 0.3)
+    opts = options(1e-4, exact_ledger=False)
+    plain = evolve(True, 40, keys, vals, terms, 0.03, 2, opts)
+    os.environ["TPGP_GB_HASH_FUSE"] = "1"
+    try:
+        fused = evolve(True, 40, keys, vals, terms, 0.03, 2, opts)
+    finally:
+        os.environ.pop("TPGP_GB_HASH_FUSE", None)
+    assert fused[0] == plain[0] == 0
+    assert np.array_equal(fused[1], plain[1])
+    assert np.array_equal(bits(fused[2]), bits(plain[2]))
+    assert np.array_equal(bits(fused[3]), bits(plain[3]))
+    assert np.array_equal(bits(ledger_vec(fused[4])), bits(ledger_vec(plain[4])))

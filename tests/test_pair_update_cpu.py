@@ -105,3 +105,61 @@ def test_pair_update_matches_reference_merge(oracle, n_spins):
         # the removed weight: the reference's sequential upward sum is an
         # upper bound of the exact sum of the same removed values
         assert led.dropped_l1 >= sum(removed) * (1 - 1e-15), trial
+
+
+def coset_run(mapping, i, j, rots, threshold):
+    """Several consecutive rotations on one site pair, applied coset by coset.
+
+    rots: [(qi, qj, c, s)].  The masks generate a group G of XOR patterns on
+    the four bits of sites i and j; K's coset K xor G is closed under every
+    rotation of the run, so each coset is updated on its own, rotation by
+    rotation with the same pair rule and the same per-rotation zero drop and
+    threshold.  Returns the kept map and the removed |v| per rotation."""
+    masks = [(qi << (2 * i)) ^ (qj << (2 * j)) for qi, qj, _, _ in rots]
+    group = {0}
+    for m in masks:
+        group |= {g ^ m for g in group}
+    site_bits = (3 << (2 * i)) | (3 << (2 * j))
+    cosets = {}
+    for K, v in mapping.items():
+        base = min(K ^ g for g in group)  # canonical member
+        cosets.setdefault(base, {})[K] = v
+    kept, removed = {}, [[] for _ in rots]
+    for members in cosets.values():
+        cur = dict(members)
+        for r, (qi, qj, c, s) in enumerate(rots):
+            new_vals, rem = pair_rotation(cur, i, j, qi, qj, c, s, threshold)
+            removed[r] += rem
+            cur = new_vals
+        kept.update(cur)
+        assert all((K & ~site_bits) == (next(iter(members)) & ~site_bits) for K in cur)
+    return kept, removed
+
+
+@pytest.mark.parametrize("n_spins", [10, 36])
+def test_edge_run_by_cosets_matches_sequential(oracle, n_spins):
+    """The three rotations of a secular edge (ZZ, XX, YY on one pair) applied
+    coset by coset equal the reference's three sequential rotations, bitwise;
+    this is what lets a future step fuse an edge's rotations into one pass."""
+    rng = np.random.default_rng(77 + n_spins)
+    words = (n_spins + 31) // 32
+    for trial in range(12):
+        keys, vals = random_map(rng, n_spins, int(rng.integers(50, 800)),
+                                active_sites=range(min(n_spins, 8)))
+        i, j = (int(x) for x in rng.choice(min(n_spins, 8), 2, replace=False))
+        d = float(rng.uniform(0.2, 1.5))
+        edge = [(3, 3, d / 2), (1, 1, -d / 4), (2, 2, -d / 4)]
+        duration = 0.05
+        threshold = float(10.0 ** rng.uniform(-6, -3))
+        rots = [(qi, qj) + oracle.trig(h, duration) for qi, qj, h in edge]
+        mapping = dict(zip(key_ints(keys, words), (float(x) for x in vals)))
+        kept, removed = coset_run(mapping, i, j, rots, threshold)
+        k, v = keys, vals
+        for qi, qj, h in edge:
+            st, k, v, led = oracle.rotate(k, v, n_spins, i, j, qi, qj, h, duration,
+                                          threshold=threshold)
+            assert st == 0
+        model_keys = sorted(kept)
+        assert model_keys == key_ints(k, words), trial
+        model_vals = np.array([kept[x] for x in model_keys], np.float64)
+        assert np.array_equal(bits(model_vals), bits(v)), trial
