@@ -55,10 +55,14 @@ typedef struct {
  *   exact_ledger = 1: the removed-weight sums are accumulated in the
  *     reference's sequential key order, so the ledger is bitwise equal to the
  *     CPU engine's; one GPU thread walks the removed terms of each rotation.
- *   exact_ledger = 0: the sums are deterministic fixed-shape trees of
- *     upward-rounded additions.  Every partial sum is rounded up, so each
- *     ledger entry is still a rigorous upper bound on the removed weight; it
- *     differs from the sequential sum by at most 3 n_removed 2^-53 relative.
+ *   exact_ledger = 0: each removed |v| and v^2 is rounded up to a multiple
+ *     of a fixed-point unit set by the threshold and summed exactly in 128-bit
+ *     integers, then converted up once per rotation: deterministic,
+ *     independent of the launch shape, a rigorous upper bound on the removed
+ *     weight a few ulps from the sequential sum.  Keys, values, FIDs and the
+ *     integer ledger fields are the same in both modes.  With this mode,
+ *     steps of maps up to 6e5 terms run the hash-table step (one kernel per
+ *     rotation, no sort; TPGP_GB_HASH=0 disables it).
  *   use_graphs = 1: each Strang step's kernel sequence is captured once as a
  *     CUDA graph and replayed. */
 typedef struct {
