@@ -18,6 +18,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import time
 
 import numpy as np
 
@@ -144,6 +145,9 @@ class Oracle:
             C.c_double, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_double),
             C.POINTER(C.c_double)]
         lib.orc_max_threads.restype = C.c_int
+        for name in ("orc_strang_bound", "orc_strang_bound_taylor"):
+            getattr(lib, name).argtypes = [C.POINTER(TermStruct), C.c_size_t, C.c_double]
+            getattr(lib, name).restype = C.c_double
         self.lib = lib
 
     # -- maps -------------------------------------------------------------
@@ -218,6 +222,26 @@ class Oracle:
     def max_threads(self):
         return self.lib.orc_max_threads()
 
+    def rotate_timed(self, keys, values, n_spins, i, j, qi, qj, h, duration, threshold=0.0,
+                     threads=1):
+        """One rotation from (keys, values); returns (status, output terms,
+        seconds spent in the C rotation call alone)."""
+        m = self._map(keys, values, n_spins)
+        led = LedgerStruct()
+        t0 = time.perf_counter()
+        st = self.lib.orc_rotate(C.byref(m), i, j, qi, qj, h, duration, threshold, 0, 0.0,
+                                 threads, C.byref(led))
+        secs = time.perf_counter() - t0
+        n_out = m.len
+        self.lib.orc_map_free(C.byref(m))
+        return st, n_out, secs
+
+    def strang_bound(self, terms, dt, taylor_only=False):
+        """Upward-rounded Strang splitting bound per step (tpgp_rev.c:875-961)."""
+        arr, count = terms_array(terms)
+        f = self.lib.orc_strang_bound_taylor if taylor_only else self.lib.orc_strang_bound
+        return f(arr, count, dt)
+
 
 class Reference:
     """The reference engine compiled from its own sources (this container only)."""
@@ -239,7 +263,30 @@ class Reference:
         lib.tpgp_map_single_sum.argtypes = [C.POINTER(MapStruct), C.c_uint]
         lib.tpgp_map_single_sum.restype = C.c_double
         lib.tpgp_ledger_init.argtypes = [C.POINTER(LedgerStruct), C.c_int]
+        for name in ("tpgp_strang_bound", "tpgp_strang_bound_taylor"):
+            getattr(lib, name).argtypes = [C.POINTER(TermStruct), C.c_size_t, C.c_double]
+            getattr(lib, name).restype = C.c_double
         self.lib = lib
+
+    def strang_bound(self, terms, dt, taylor_only=False):
+        arr, count = terms_array(terms)
+        f = self.lib.tpgp_strang_bound_taylor if taylor_only else self.lib.tpgp_strang_bound
+        return f(arr, count, dt)
+
+    def rotate_timed(self, keys, values, n_spins, i, j, qi, qj, h, duration, threshold=0.0,
+                     threads=1):
+        """tpgp_rotate of h * duration (OpenMP backend with `threads`) from
+        (keys, values); returns (status, output terms, seconds of the call)."""
+        m = self._map(keys, values, n_spins)
+        o = self.options(threshold, 0, 0.0, threads, 2 if threads > 1 else 0)
+        led = LedgerStruct()
+        t0 = time.perf_counter()
+        st = self.lib.tpgp_rotate(C.byref(m), i, j, qi, qj, h * duration, C.byref(o),
+                                  C.byref(led))
+        secs = time.perf_counter() - t0
+        n_out = m.len
+        self.lib.tpgp_map_free(C.byref(m))
+        return st, n_out, secs
 
     def options(self, threshold=0.0, max_terms=0, max_drop_l2=0.0, threads=1, backend=0):
         o = self.lib.tpgp_default_options()

@@ -444,3 +444,123 @@ int orc_max_threads(void) {
     return 1;
 #endif
 }
+
+/* ---------------------------------------------------------------------------
+ * Strang splitting error bound per step (tpgp_rev.c:875-961), the pf term of
+ * the CLI's observable bound (cli_rev.c:549-587).  Every sum and product is
+ * rounded upward (up_add/up_mul) in the reference's order, so the result is
+ * bitwise the reference's.
+ *
+ * Taylor bound: (2/3) (lambda |dt|)^3 with lambda = sum |h_k| (tpgp_rev.c:875-890).
+ * Commutator bound: 2 C |dt|^3 with
+ *   C = sum_a [ h_a^2 (sum_{b in N(a), b > a} |h_b|) / 6
+ *              + sum_{b in N(a), b > a} |h_a h_b| (sum_{c in N(a) xor N(b), c > a} |h_c|) / 3 ]
+ * where N(a) are the terms that anticommute with term a (both h nonzero),
+ * ascending; the bound is the smaller of the two (tpgp_rev.c:891-961). */
+static int single_anticommutes(unsigned q, unsigned p) { return q && p && q != p; }
+
+static int terms_anticommute(const orc_term *a, const orc_term *b) {
+    int odd = 0;
+    if (a->i == b->i) odd ^= single_anticommutes(a->qi, b->qi);
+    if (a->i == b->j) odd ^= single_anticommutes(a->qi, b->qj);
+    if (a->j == b->i) odd ^= single_anticommutes(a->qj, b->qi);
+    if (a->j == b->j) odd ^= single_anticommutes(a->qj, b->qj);
+    return odd;
+}
+
+double orc_strang_bound_taylor(const orc_term *terms, size_t count, double dt) {
+    if ((!terms && count) || !isfinite(dt))
+        return NAN;
+    double lambda = 0;
+    for (size_t k = 0; k < count; k++) {
+        const orc_term *t = terms + k;
+        if (!isfinite(t->h) || t->i == t->j || t->qi > 3 || t->qj > 3)
+            return NAN;
+        lambda = up_add(lambda, fabs(t->h));
+    }
+    const double x = up_mul(lambda, fabs(dt));
+    return up_mul(up_mul(up_mul(x, x), x), nextafter(2.0 / 3.0, INFINITY));
+}
+
+double orc_strang_bound(const orc_term *terms, size_t count, double dt) {
+    const double taylor = orc_strang_bound_taylor(terms, count, dt);
+    if (isnan(taylor))
+        return NAN;
+    /* anticommutation graph as a CSR structure, rows ascending */
+    size_t *degree = calloc(count + 1, sizeof(size_t));
+    if (!degree)
+        return taylor;
+    for (size_t a = 0; a < count; a++)
+        for (size_t b = a + 1; b < count; b++)
+            if (terms[a].h != 0 && terms[b].h != 0 && terms_anticommute(terms + a, terms + b)) {
+                degree[a]++;
+                degree[b]++;
+            }
+    size_t *start = malloc((count + 1) * sizeof(size_t));
+    size_t total = 0;
+    for (size_t a = 0; a < count; a++)
+        total += degree[a];
+    size_t *adj = malloc((total ? total : 1) * sizeof(size_t));
+    size_t *fill = calloc(count + 1, sizeof(size_t));
+    if (!start || !adj || !fill) {
+        free(degree);
+        free(start);
+        free(adj);
+        free(fill);
+        return taylor;
+    }
+    start[0] = 0;
+    for (size_t a = 0; a < count; a++)
+        start[a + 1] = start[a] + degree[a];
+    /* pairs in (a ascending, b ascending) order keep every row sorted */
+    for (size_t a = 0; a < count; a++)
+        for (size_t b = a + 1; b < count; b++)
+            if (terms[a].h != 0 && terms[b].h != 0 && terms_anticommute(terms + a, terms + b)) {
+                adj[start[a] + fill[a]++] = b;
+                adj[start[b] + fill[b]++] = a;
+            }
+    const double sixth = nextafter(1.0 / 6.0, INFINITY), third = nextafter(1.0 / 3.0, INFINITY);
+    double C = 0;
+    for (size_t a = 0; a < count; a++) {
+        const double ha = fabs(terms[a].h);
+        const size_t *na = adj + start[a];
+        const size_t da = degree[a];
+        double later = 0;
+        for (size_t k = 0; k < da; k++)
+            if (na[k] > a)
+                later = up_add(later, fabs(terms[na[k]].h));
+        C = up_add(C, up_mul(up_mul(up_mul(ha, ha), later), sixth));
+        for (size_t k = 0; k < da; k++) {
+            const size_t b = na[k];
+            if (b <= a)
+                continue;
+            const size_t *nb = adj + start[b];
+            const size_t db = degree[b];
+            size_t x = 0, y = 0;
+            double odd = 0;
+            /* ascending walk over N(a) xor N(b) */
+            while (x < da || y < db) {
+                size_t c;
+                if (y == db || (x < da && na[x] < nb[y])) {
+                    c = na[x++];
+                } else if (x == da || nb[y] < na[x]) {
+                    c = nb[y++];
+                } else {
+                    x++;
+                    y++;
+                    continue;
+                }
+                if (c > a)
+                    odd = up_add(odd, fabs(terms[c].h));
+            }
+            C = up_add(C, up_mul(up_mul(up_mul(ha, fabs(terms[b].h)), odd), third));
+        }
+    }
+    free(degree);
+    free(start);
+    free(adj);
+    free(fill);
+    const double t = fabs(dt);
+    const double nested = up_mul(up_mul(up_mul(up_mul(2, C), t), t), t);
+    return fmin(taylor, nested);
+}

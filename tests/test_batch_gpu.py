@@ -152,3 +152,45 @@ def test_cta_table_overflow_falls_back(engine):
         assert led1.as_dict() == batch.ledger(item).as_dict(), item
     assert batch.item_len(0) > 4096
     batch.close()
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_batch_items_match_oracle(engine, oracle, exact):
+    """Each item against the CPU oracle (the reference algorithm) on its own
+    inputs: powder items as the batched benchmark builds them -- cubic
+    fragments of 8..64 spins (one- and two-word keys) whose couplings are
+    rescaled by their own field direction, dt = 0.01, threshold 1e-5.  Keys,
+    values and per-step FIDs bitwise; the ledger bitwise with the exact
+    ledger; with the fixed-point ledger the removed-weight sums (an upper
+    bound of the exact sums, like the reference's sequential upward sums)
+    within a few ulps of the reference's."""
+    sizes = [8, 13, 24, 31, 32, 33, 40, 50, 64, 64]
+    dirs = H.sphere_directions(len(sizes), seed=20260711)
+    items = [(n, H.cubic_fragment(n, d)) for n, d in zip(sizes, dirs)]
+    steps, dt, thr = 6, 0.01, 1e-5
+    batch = Batch(engine, [n for n, _ in items])
+    for k, (n, terms) in enumerate(items):
+        batch.upload(k, *H.single_site_operator(n, 0))
+        batch.set_terms(k, terms, dt, options(thr, exact_ledger=exact))
+    fids = batch.step(steps)
+    for k, (n, terms) in enumerate(items):
+        assert batch.item_status(k) == 0
+        fo = []
+        st, ok, ov, oled = oracle.strang_step(*H.single_site_operator(n, 0), n, terms, dt,
+                                              threshold=thr, steps=steps,
+                                              on_step=lambda s, f, nn: fo.append(f))
+        assert st == 0
+        kb, vb = batch.download(k)
+        assert np.array_equal(kb, ok), k
+        assert np.array_equal(bits(vb), bits(ov)), k
+        assert np.array_equal(bits(fids[:, k]), bits(fo)), k
+        led = batch.ledger(k)
+        assert (led.rotations, led.removal_events, led.peak_terms) == \
+            (oled.rotations, oled.removal_events, oled.peak_terms), k
+        for f in ("dropped_l1", "dropped_l2", "dropped_l2_squared"):
+            a, b = getattr(led, f), getattr(oled, f)
+            if exact:
+                assert bits([a]) == bits([b]), (k, f)
+            else:  # both are upper bounds of the exact sum, a few ulps apart
+                assert abs(a - b) <= 1e-11 * b, (k, f)
+    batch.close()

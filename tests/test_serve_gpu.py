@@ -59,3 +59,22 @@ def test_queueing_reuses_slots(engine):
     assert all(x["status"] == 0 for x in resp)
     # with one slot per width, some request had to wait for a slot
     assert max(x["admitted"] - q["arrival"] for x, q in zip(resp, reqs)) > 0
+
+
+def test_served_fids_match_oracle_at_true_size(engine, oracle):
+    """Each served request against the CPU oracle run at the request's own
+    spin count (the server widens a request to its slot's 32/64/96 spins):
+    per-step FIDs bitwise, requests of all three key widths, one of them
+    run for 30 steps."""
+    reqs = make_requests(9, seed=14)
+    reqs[0]["steps"] = 30
+    assert {(q["n_spins"] + 31) // 32 for q in reqs} == {1, 2, 3}
+    resp, fids, _ = engine.serve(reqs, slots=(2, 2, 2))
+    for r, q in enumerate(reqs):
+        assert resp[r]["status"] == 0
+        fo = []
+        st, _, _, _ = oracle.strang_step(q["keys"], q["values"], q["n_spins"], q["terms"], q["dt"],
+                                         threshold=q["options"].threshold, steps=q["steps"],
+                                         on_step=lambda s, f, n: fo.append(f))
+        assert st == 0
+        assert np.array_equal(fids[r].view(np.uint64), np.array(fo).view(np.uint64)), r
