@@ -1,14 +1,24 @@
 // Reference-compatible CUDA branch backend (include/tpgp_cuda_rev.h).
 //
-// Same contract as DDevol engine/src/cuda_rev.cu:117-272: host arrays in,
-// two raw children per term out in the serial engine's slot order, host
-// trigonometric factors, persistent device scratch, calls on one context
-// serialised.  The kernel is written for sm_103a: one thread per term, keys
-// of one or two words move as single 64/128-bit vector accesses, a term's
-// two coefficients and two radii are written as one 16-byte store each, and
+// Contract (DDevol engine/include/tpgp_cuda_rev.h:9-48, the statuses and
+// argument rules its engine relies on at engine/src/tpgp_rev.c:622-640):
+// host arrays in, two raw children per term out in the serial engine's slot
+// order, trigonometric factors from the host, persistent device scratch per
+// context, calls on one context serialised, the caller's current device
+// restored.  The kernel is written for sm_103a: one thread per term, keys of
+// one or two words move as single 64/128-bit vector accesses, a term's two
+// coefficients and two radii are written as one 16-byte store each, and
 // failure flags are reduced per warp (ballot) before one atomic.
+//
+// Host side: a call is first turned into a BranchPlan (every argument rule
+// checked, byte sizes computed without overflow); the plan fixes the
+// staging layout on the device; a StepRunner then issues the transfers and
+// the launch on one stream and stops at the first CUDA error.  The context
+// path stages through a growing DeviceScratch; the allocation-free path
+// stages through a static device array.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -16,6 +26,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <cstdarg>
 #include <mutex>
 
 #include "../../include/tpgp_cuda_rev.h"
@@ -24,40 +35,8 @@
 static_assert(sizeof(double) == 8 && DBL_MANT_DIG == 53 && FLT_RADIX == 2,
               "the branch backend requires IEEE binary64");
 
-struct tpgp_cuda_context {
-    int device;
-    int sms;
-    cudaStream_t stream;
-    void* scratch;
-    size_t scratch_bytes;
-    std::mutex lock;
-    char name[256];
-};
 
 namespace {
-
-void set_message(char* error, size_t cap, const char* text) {
-    if (error && cap) std::snprintf(error, cap, "%s", text);
-}
-tpgp_cuda_status cuda_failure(cudaError_t code, const char* what, char* error, size_t cap) {
-    if (error && cap) std::snprintf(error, cap, "%s: %s", what, cudaGetErrorString(code));
-    return code == cudaErrorMemoryAllocation ? TPGP_CUDA_ENOMEM : TPGP_CUDA_EDEVICE;
-}
-bool mul_ok(size_t a, size_t b, size_t* out) {
-    if (b && a > SIZE_MAX / b) return false;
-    *out = a * b;
-    return true;
-}
-bool add_ok(size_t a, size_t b, size_t* out) {
-    if (a > SIZE_MAX - b) return false;
-    *out = a + b;
-    return true;
-}
-bool ranges_overlap(const void* a, size_t as, const void* b, size_t bs) {
-    const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
-    if (as > UINTPTR_MAX - x || bs > UINTPTR_MAX - y) return true;
-    return x < y + bs && y < x + as;
-}
 
 // Largest |x - neighbour| over the two adjacent binary64 values: the
 // rounding radius of the serial engine (engine/src/tpgp_rev.c:37-42).
@@ -145,51 +124,309 @@ __global__ void __launch_bounds__(256)
 
 }  // namespace
 
+
+// ============================================================ host side
+namespace {
+
+// Writes the caller's message buffer (always NUL-terminated, may be NULL).
+class Report {
+  public:
+    Report(char* buffer, size_t capacity) : buf_(buffer), cap_(capacity) {
+        if (buf_ && cap_) buf_[0] = '\0';
+    }
+    tpgp_cuda_status fail(tpgp_cuda_status status, const char* format, ...) {
+        if (buf_ && cap_) {
+            va_list args;
+            va_start(args, format);
+            std::vsnprintf(buf_, cap_, format, args);
+            va_end(args);
+        }
+        return status;
+    }
+    // Allocation failures map to ENOMEM, every other CUDA error to EDEVICE.
+    tpgp_cuda_status cuda(cudaError_t code, const char* stage) {
+        return fail(code == cudaErrorMemoryAllocation ? TPGP_CUDA_ENOMEM : TPGP_CUDA_EDEVICE,
+                    "tpgp_cuda: %s failed (%s)", stage, cudaGetErrorString(code));
+    }
+
+  private:
+    char* buf_;
+    size_t cap_;
+};
+
+// A validated call: geometry, generator, factors and byte sizes.
+struct BranchPlan {
+    size_t count = 0, words = 0, spins = 0, i = 0, j = 0;
+    unsigned qi = 0, qj = 0;
+    double c = 0, s = 0, rc = 0, rs = 0;
+    int enclose = 0;
+    size_t key_bytes = 0;    // count * words * 8 (input keys)
+    size_t value_bytes = 0;  // count * 8 (input coefficients)
+};
+
+bool product(size_t a, size_t b, size_t& out) {
+    if (b != 0 && a > SIZE_MAX / b) return false;
+    out = a * b;
+    return true;
+}
+
+bool intersects(const void* a, size_t a_bytes, const void* b, size_t b_bytes) {
+    const uintptr_t pa = reinterpret_cast<uintptr_t>(a), pb = reinterpret_cast<uintptr_t>(b);
+    if (a_bytes > UINTPTR_MAX - pa || b_bytes > UINTPTR_MAX - pb) return true;  // wraps: reject
+    return pa < pb + b_bytes && pb < pa + a_bytes;
+}
+
+// The geometry and generator rules (checked before anything else, also for
+// an empty call): at least two spins, words = ceil(spins / 32), two distinct
+// sites below spins, Pauli labels 0..3, finite factors, non-negative
+// enclosure radii, enclose 0 or 1.
+bool valid_geometry(size_t words, size_t spins, size_t i, size_t j, unsigned qi, unsigned qj,
+                    double c, double s, double rc, double rs, int enclose) {
+    const bool sizes = spins >= 2 && words == (spins + 31) / 32;
+    const bool sites = i < spins && j < spins && i != j;
+    const bool labels = qi <= 3 && qj <= 3;
+    const bool factors = std::isfinite(c) && std::isfinite(s) && std::isfinite(rc) &&
+                         std::isfinite(rs) && rc >= 0 && rs >= 0;
+    return sizes && sites && labels && factors && (enclose == 0 || enclose == 1);
+}
+
+// Fills `plan` for a non-empty call after valid_geometry: rejects NULL
+// arrays, byte counts that overflow, and overlapping host arrays.
+tpgp_cuda_status plan_arrays(BranchPlan& plan, const uint64_t* keys, const double* values,
+                             const uint64_t* out_keys, const double* out_values,
+                             const double* out_radii, Report& report) {
+    // every byte count below (staging is at most 3 key_bytes + 5 value_bytes
+    // + 96) stays below SIZE_MAX when key_bytes and value_bytes are below SIZE_MAX / 16
+    size_t key_words = 0, child_key_bytes = 0, child_value_bytes = 0, headroom = 0;
+    const bool sized = product(plan.count, plan.words, key_words) &&
+                       product(key_words, 8, plan.key_bytes) &&
+                       product(plan.count, 8, plan.value_bytes) &&
+                       product(plan.key_bytes, 16, headroom) &&
+                       product(plan.value_bytes, 16, headroom);
+    child_key_bytes = 2 * plan.key_bytes;
+    child_value_bytes = 2 * plan.value_bytes;
+    if (!keys || !values || !out_keys || !out_values || !out_radii)
+        return report.fail(TPGP_CUDA_EINVAL, "tpgp_cuda: %zu terms but a NULL array", plan.count);
+    if (!sized)
+        return report.fail(TPGP_CUDA_EINVAL, "tpgp_cuda: %zu terms of %zu words overflow size_t",
+                           plan.count, plan.words);
+    const void* arrays[5] = {keys, values, out_keys, out_values, out_radii};
+    const size_t bytes[5] = {plan.key_bytes, plan.value_bytes, child_key_bytes,
+                             child_value_bytes, child_value_bytes};
+    for (int a = 0; a < 5; ++a)
+        for (int b = a + 1; b < 5; ++b)
+            if (intersects(arrays[a], bytes[a], arrays[b], bytes[b]))
+                return report.fail(TPGP_CUDA_EINVAL,
+                                   "tpgp_cuda: host arrays %d and %d overlap (inputs keys, "
+                                   "values; outputs keys, values, radii)", a, b);
+    return TPGP_CUDA_OK;
+}
+
+// Device staging of one call, 16-byte aligned regions in one block:
+// children's keys, values and radii, the input keys and values, the flag.
+struct Staging {
+    size_t child_keys, child_values, child_radii, in_keys, in_values, flag, bytes;
+    explicit Staging(const BranchPlan& p) {
+        auto next = [](size_t at, size_t len) { return (at + len + 15) & ~size_t(15); };
+        child_keys = 0;
+        child_values = next(child_keys, 2 * p.key_bytes);
+        child_radii = next(child_values, 2 * p.value_bytes);
+        in_keys = next(child_radii, 2 * p.value_bytes);
+        in_values = next(in_keys, p.key_bytes);
+        flag = next(in_values, p.value_bytes);
+        bytes = flag + 16;
+    }
+};
+
+// Selects a device for the lifetime of the object and puts the caller's
+// current device back (restore() reports a failure to do so).
+class DeviceScope {
+  public:
+    cudaError_t enter(int device) {
+        cudaError_t e = cudaGetDevice(&previous_);
+        if (e == cudaSuccess) e = cudaSetDevice(device);
+        active_ = e == cudaSuccess;
+        return e;
+    }
+    cudaError_t restore() {
+        if (!active_) return cudaSuccess;
+        active_ = false;
+        return cudaSetDevice(previous_);
+    }
+    ~DeviceScope() { restore(); }
+
+  private:
+    int previous_ = 0;
+    bool active_ = false;
+};
+
+// Growing device allocation kept between calls (nothing lives in it across
+// calls, so growing frees the old block before allocating the new one).
+class DeviceScratch {
+  public:
+    cudaError_t reserve(size_t bytes) {
+        if (bytes <= bytes_) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&ptr_, bytes);
+        if (e != cudaSuccess) {
+            ptr_ = nullptr;
+            return e;
+        }
+        bytes_ = bytes;
+        return cudaSuccess;
+    }
+    void release() {
+        if (ptr_) cudaFree(ptr_);
+        ptr_ = nullptr;
+        bytes_ = 0;
+    }
+    unsigned char* data() const { return static_cast<unsigned char*>(ptr_); }
+
+  private:
+    void* ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// Runs CUDA calls in order until the first error, which it reports.
+class StepRunner {
+  public:
+    explicit StepRunner(Report& report) : report_(report) {}
+    template <class Call>
+    StepRunner& then(const char* stage, Call&& call) {
+        if (status_ == TPGP_CUDA_OK) {
+            const cudaError_t e = call();
+            if (e != cudaSuccess) status_ = report_.cuda(e, stage);
+        }
+        return *this;
+    }
+    bool ok() const { return status_ == TPGP_CUDA_OK; }
+    tpgp_cuda_status status() const { return status_; }
+
+  private:
+    Report& report_;
+    tpgp_cuda_status status_ = TPGP_CUDA_OK;
+};
+
+void launch_branch(const BranchPlan& p, unsigned char* base, const Staging& at, int sms,
+                   cudaStream_t stream) {
+    const size_t blocks_wanted = (p.count + 255) / 256, blocks_max = (size_t)std::max(sms, 1) * 16;
+    const unsigned blocks = (unsigned)std::min(blocks_wanted, blocks_max);
+    auto* ck = reinterpret_cast<uint64_t*>(base + at.child_keys);
+    auto* cv = reinterpret_cast<double*>(base + at.child_values);
+    auto* cr = reinterpret_cast<double*>(base + at.child_radii);
+    auto* ik = reinterpret_cast<const uint64_t*>(base + at.in_keys);
+    auto* iv = reinterpret_cast<const double*>(base + at.in_values);
+    auto* flag = reinterpret_cast<unsigned*>(base + at.flag);
+#define TPGP_BRANCH_LAUNCH(W)                                                                    \
+    k_branch<W><<<blocks, 256, 0, stream>>>(ik, iv, p.count, p.words, p.spins, p.i, p.j, p.qi,   \
+                                            p.qj, p.c, p.s, p.rc, p.rs, p.enclose, ck, cv, cr,   \
+                                            flag)
+    if (p.words == 1) TPGP_BRANCH_LAUNCH(1);
+    else if (p.words == 2) TPGP_BRANCH_LAUNCH(2);
+    else TPGP_BRANCH_LAUNCH(0);
+#undef TPGP_BRANCH_LAUNCH
+}
+
+// Stages one planned call through `base` on `stream`: inputs up, flag
+// cleared, kernel, then the flag and all children down in one go and a
+// single wait.  The children reach the caller's arrays even when the flag
+// reports a failure; the contract makes outputs valid only on success.
+tpgp_cuda_status run_branch(const BranchPlan& p, unsigned char* base, int sms, cudaStream_t stream,
+                            const uint64_t* keys, const double* values, uint64_t* out_keys,
+                            double* out_values, double* out_radii, Report& report) {
+    const Staging at(p);
+    unsigned flag = 0;
+    StepRunner run(report);
+    run.then("input key upload", [&] {
+           return cudaMemcpyAsync(base + at.in_keys, keys, p.key_bytes, cudaMemcpyHostToDevice,
+                                  stream);
+       })
+        .then("input coefficient upload", [&] {
+            return cudaMemcpyAsync(base + at.in_values, values, p.value_bytes,
+                                   cudaMemcpyHostToDevice, stream);
+        })
+        .then("failure flag reset", [&] { return cudaMemsetAsync(base + at.flag, 0, 4, stream); })
+        .then("branch kernel launch", [&] {
+            launch_branch(p, base, at, sms, stream);
+            return cudaGetLastError();
+        })
+        .then("failure flag download", [&] {
+            return cudaMemcpyAsync(&flag, base + at.flag, 4, cudaMemcpyDeviceToHost, stream);
+        })
+        .then("child key download", [&] {
+            return cudaMemcpyAsync(out_keys, base + at.child_keys, 2 * p.key_bytes,
+                                   cudaMemcpyDeviceToHost, stream);
+        })
+        .then("child coefficient download", [&] {
+            return cudaMemcpyAsync(out_values, base + at.child_values, 2 * p.value_bytes,
+                                   cudaMemcpyDeviceToHost, stream);
+        })
+        .then("child radius download", [&] {
+            return cudaMemcpyAsync(out_radii, base + at.child_radii, 2 * p.value_bytes,
+                                   cudaMemcpyDeviceToHost, stream);
+        })
+        .then("branch execution", [&] { return cudaStreamSynchronize(stream); });
+    if (!run.ok()) {
+        cudaStreamSynchronize(stream);  // nothing may still target the caller's arrays
+        return run.status();
+    }
+    if (flag & 1u)
+        return report.fail(TPGP_CUDA_EINVAL,
+                           "tpgp_cuda: an input key sets bits above site %zu", p.spins - 1);
+    if (flag & 2u)
+        return report.fail(TPGP_CUDA_ENUMERIC,
+                           "tpgp_cuda: a coefficient, child or radius is not finite");
+    return TPGP_CUDA_OK;
+}
+
+}  // namespace
+
+struct tpgp_cuda_context {
+    int device = 0;
+    int sms = 1;
+    cudaStream_t stream = nullptr;
+    DeviceScratch scratch;
+    std::mutex lock;  // serialises calls on this context
+    char name[256] = {};
+};
+
 extern "C" int tpgp_cuda_compiled(void) { return 1; }
 
 extern "C" tpgp_cuda_context* tpgp_cuda_create(int index, char* error, size_t cap) {
-    set_message(error, cap, "");
-    int count = 0, previous = 0;
-    cudaError_t code = cudaGetDeviceCount(&count);
-    if (code != cudaSuccess) {
-        cuda_failure(code, "CUDA device discovery", error, cap);
+    Report report(error, cap);
+    int devices = 0;
+    cudaError_t e = cudaGetDeviceCount(&devices);
+    if (e != cudaSuccess) {
+        report.cuda(e, "device count");
         return nullptr;
     }
-    if (index < 0 || index >= count) {
-        set_message(error, cap, "Requested CUDA device index is unavailable.");
-        return nullptr;
-    }
-    if ((code = cudaGetDevice(&previous)) != cudaSuccess) {
-        cuda_failure(code, "CUDA current-device query", error, cap);
-        return nullptr;
-    }
-    if ((code = cudaSetDevice(index)) != cudaSuccess) {
-        cuda_failure(code, "CUDA device selection", error, cap);
+    if (index < 0 || index >= devices) {
+        report.fail(TPGP_CUDA_EINVAL, "tpgp_cuda: device %d requested, %d visible", index, devices);
         return nullptr;
     }
     cudaDeviceProp prop;
-    if ((code = cudaGetDeviceProperties(&prop, index)) != cudaSuccess) {
-        cuda_failure(code, "CUDA device properties", error, cap);
-        cudaSetDevice(previous);
+    if ((e = cudaGetDeviceProperties(&prop, index)) != cudaSuccess) {
+        report.cuda(e, "device properties");
         return nullptr;
     }
     auto* ctx = new (std::nothrow) tpgp_cuda_context();
     if (!ctx) {
-        set_message(error, cap, "Could not allocate the CUDA host context.");
-        cudaSetDevice(previous);
+        report.fail(TPGP_CUDA_ENOMEM, "tpgp_cuda: out of host memory for the context");
         return nullptr;
     }
     ctx->device = index;
-    ctx->sms = prop.multiProcessorCount > 0 ? prop.multiProcessorCount : 1;
-    std::snprintf(ctx->name, sizeof(ctx->name), "%s (sm_%d%d)", prop.name, prop.major, prop.minor);
-    if ((code = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
-        cuda_failure(code, "CUDA stream creation", error, cap);
+    ctx->sms = std::max(prop.multiProcessorCount, 1);
+    std::snprintf(ctx->name, sizeof(ctx->name), "%.200s (sm_%d%d)", prop.name, prop.major,
+                  prop.minor);
+    DeviceScope scope;
+    if ((e = scope.enter(index)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        report.cuda(e, "stream set-up");
         delete ctx;
-        cudaSetDevice(previous);
         return nullptr;
     }
-    if ((code = cudaSetDevice(previous)) != cudaSuccess) {
-        cuda_failure(code, "CUDA previous-device restoration", error, cap);
+    if ((e = scope.restore()) != cudaSuccess) {
+        report.cuda(e, "restoring the caller's device");
         cudaStreamDestroy(ctx->stream);
         delete ctx;
         return nullptr;
@@ -199,13 +436,14 @@ extern "C" tpgp_cuda_context* tpgp_cuda_create(int index, char* error, size_t ca
 
 extern "C" void tpgp_cuda_destroy(tpgp_cuda_context* ctx) {
     if (!ctx) return;
-    int previous = ctx->device;
-    cudaGetDevice(&previous);
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    if (ctx->scratch) cudaFree(ctx->scratch);
-    cudaStreamDestroy(ctx->stream);
-    cudaSetDevice(previous);
+    {
+        DeviceScope scope;
+        if (scope.enter(ctx->device) == cudaSuccess) {
+            cudaStreamSynchronize(ctx->stream);
+            ctx->scratch.release();
+            cudaStreamDestroy(ctx->stream);
+        }
+    }
     delete ctx;
 }
 
@@ -220,134 +458,31 @@ extern "C" tpgp_cuda_status tpgp_cuda_branches(tpgp_cuda_context* ctx, const uin
                                                double rs, int enclose, uint64_t* out_keys,
                                                double* out_values, double* out_radii,
                                                char* error, size_t cap) {
-    set_message(error, cap, "");
-    // argument checks of engine/src/cuda_rev.cu:180-203, in the same order
-    if (!ctx || spins < 2 || words != spins / 32 + (spins % 32 != 0) || i >= spins ||
-        j >= spins || i == j || qi > 3 || qj > 3 || !std::isfinite(c) || !std::isfinite(s) ||
-        !std::isfinite(rc) || !std::isfinite(rs) || rc < 0 || rs < 0 ||
-        (enclose != 0 && enclose != 1)) {
-        set_message(error, cap,
-                    "Invalid CUDA branch dimensions, sites, generator, or trigonometric enclosure.");
-        return TPGP_CUDA_EINVAL;
-    }
-    if (!count) return TPGP_CUDA_OK;
-    size_t key_bytes, value_bytes, out_key_bytes, out_value_bytes, total, t;
-    if (!keys || !values || !out_keys || !out_values || !out_radii || !mul_ok(count, words, &t) ||
-        !mul_ok(t, sizeof(uint64_t), &key_bytes) || !mul_ok(count, sizeof(double), &value_bytes) ||
-        !mul_ok(key_bytes, 2, &out_key_bytes) || !mul_ok(value_bytes, 2, &out_value_bytes) ||
-        !mul_ok(key_bytes, 3, &total) || !mul_ok(value_bytes, 5, &t) || !add_ok(total, t, &total) ||
-        !add_ok(total, 64, &total)) {
-        set_message(error, cap, "Null CUDA array or packed-branch allocation size overflow.");
-        return TPGP_CUDA_EINVAL;
-    }
-    const void* arrays[] = {keys, values, out_keys, out_values, out_radii};
-    const size_t lengths[] = {key_bytes, value_bytes, out_key_bytes, out_value_bytes,
-                              out_value_bytes};
-    for (int x = 0; x < 5; ++x)
-        for (int y = x + 1; y < 5; ++y)
-            if (ranges_overlap(arrays[x], lengths[x], arrays[y], lengths[y])) {
-                set_message(error, cap, "CUDA input/output arrays must be disjoint.");
-                return TPGP_CUDA_EINVAL;
-            }
+    Report report(error, cap);
+    if (!ctx)
+        return report.fail(TPGP_CUDA_EINVAL, "tpgp_cuda: NULL context");
+    if (!valid_geometry(words, spins, i, j, qi, qj, c, s, rc, rs, enclose))
+        return report.fail(TPGP_CUDA_EINVAL,
+                           "tpgp_cuda: invalid rotation (spins %zu, words %zu, sites %zu/%zu, "
+                           "labels %u/%u, factors or enclose flag)", spins, words, i, j, qi, qj);
+    if (count == 0) return TPGP_CUDA_OK;  // NULL arrays are fine for an empty call
+    BranchPlan plan;
+    plan.count = count, plan.words = words, plan.spins = spins, plan.i = i, plan.j = j;
+    plan.qi = qi, plan.qj = qj, plan.c = c, plan.s = s, plan.rc = rc, plan.rs = rs;
+    plan.enclose = enclose;
+    tpgp_cuda_status st = plan_arrays(plan, keys, values, out_keys, out_values, out_radii, report);
+    if (st != TPGP_CUDA_OK) return st;
     std::lock_guard<std::mutex> guard(ctx->lock);
-    tpgp_cuda_status result = TPGP_CUDA_OK;
-    int previous = ctx->device;
-    cudaError_t code = cudaGetDevice(&previous);
-    if (code != cudaSuccess) result = cuda_failure(code, "CUDA current-device query", error, cap);
-    if (result == TPGP_CUDA_OK && (code = cudaSetDevice(ctx->device)) != cudaSuccess)
-        result = cuda_failure(code, "CUDA device selection", error, cap);
-    if (result == TPGP_CUDA_OK && total > ctx->scratch_bytes) {
-        // nothing lives in the scratch between calls: release before growing
-        if (ctx->scratch) {
-            code = cudaFree(ctx->scratch);
-            ctx->scratch = nullptr;
-            ctx->scratch_bytes = 0;
-            if (code != cudaSuccess) result = cuda_failure(code, "CUDA scratch release", error, cap);
-        }
-        if (result == TPGP_CUDA_OK) {
-            if ((code = cudaMalloc(&ctx->scratch, total)) != cudaSuccess) {
-                ctx->scratch = nullptr;
-                result = cuda_failure(code, "CUDA persistent scratch allocation", error, cap);
-            } else {
-                ctx->scratch_bytes = total;
-            }
-        }
-    }
-    if (result == TPGP_CUDA_OK) {
-        // 16-byte aligned sub-buffers: out keys, out values, out radii, in keys, in values, flags
-        unsigned char* base = static_cast<unsigned char*>(ctx->scratch);
-        auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
-        size_t off = 0;
-        uint64_t* d_out_keys = reinterpret_cast<uint64_t*>(base + off);
-        off = align16(off + out_key_bytes);
-        double* d_out_values = reinterpret_cast<double*>(base + off);
-        off = align16(off + out_value_bytes);
-        double* d_out_radii = reinterpret_cast<double*>(base + off);
-        off = align16(off + out_value_bytes);
-        uint64_t* d_keys = reinterpret_cast<uint64_t*>(base + off);
-        off = align16(off + key_bytes);
-        double* d_values = reinterpret_cast<double*>(base + off);
-        off = align16(off + value_bytes);
-        unsigned* d_failure = reinterpret_cast<unsigned*>(base + off);
-        unsigned failure = 0;
-#define STEP(call, what)                                                      \
-    do {                                                                      \
-        if (result == TPGP_CUDA_OK) {                                         \
-            code = (call);                                                    \
-            if (code != cudaSuccess) result = cuda_failure(code, what, error, cap); \
-        }                                                                     \
-    } while (0)
-        STEP(cudaMemcpyAsync(d_keys, keys, key_bytes, cudaMemcpyHostToDevice, ctx->stream),
-             "CUDA input-key transfer");
-        STEP(cudaMemcpyAsync(d_values, values, value_bytes, cudaMemcpyHostToDevice, ctx->stream),
-             "CUDA input-coefficient transfer");
-        STEP(cudaMemsetAsync(d_failure, 0, sizeof(unsigned), ctx->stream), "CUDA status reset");
-        if (result == TPGP_CUDA_OK) {
-            const size_t want = (count + 255) / 256;
-            const size_t cap_blocks = (size_t)ctx->sms * 16;
-            const unsigned blocks = (unsigned)(want < cap_blocks ? want : cap_blocks);
-            if (words == 1)
-                k_branch<1><<<blocks, 256, 0, ctx->stream>>>(
-                    d_keys, d_values, count, words, spins, i, j, qi, qj, c, s, rc, rs, enclose,
-                    d_out_keys, d_out_values, d_out_radii, d_failure);
-            else if (words == 2)
-                k_branch<2><<<blocks, 256, 0, ctx->stream>>>(
-                    d_keys, d_values, count, words, spins, i, j, qi, qj, c, s, rc, rs, enclose,
-                    d_out_keys, d_out_values, d_out_radii, d_failure);
-            else
-                k_branch<0><<<blocks, 256, 0, ctx->stream>>>(
-                    d_keys, d_values, count, words, spins, i, j, qi, qj, c, s, rc, rs, enclose,
-                    d_out_keys, d_out_values, d_out_radii, d_failure);
-            STEP(cudaGetLastError(), "CUDA branch-kernel launch");
-        }
-        STEP(cudaMemcpyAsync(&failure, d_failure, sizeof(unsigned), cudaMemcpyDeviceToHost,
-                             ctx->stream),
-             "CUDA status transfer");
-        STEP(cudaStreamSynchronize(ctx->stream), "CUDA branch-kernel execution");
-        if (result == TPGP_CUDA_OK && failure) {
-            result = (failure & 1u) ? TPGP_CUDA_EINVAL : TPGP_CUDA_ENUMERIC;
-            set_message(error, cap,
-                        (failure & 1u) ? "CUDA input keys contain nonzero padding bits."
-                                       : "CUDA branch arithmetic or coefficients are nonfinite.");
-        }
-        STEP(cudaMemcpyAsync(out_keys, d_out_keys, out_key_bytes, cudaMemcpyDeviceToHost,
-                             ctx->stream),
-             "CUDA output-key transfer");
-        STEP(cudaMemcpyAsync(out_values, d_out_values, out_value_bytes, cudaMemcpyDeviceToHost,
-                             ctx->stream),
-             "CUDA output-coefficient transfer");
-        STEP(cudaMemcpyAsync(out_radii, d_out_radii, out_value_bytes, cudaMemcpyDeviceToHost,
-                             ctx->stream),
-             "CUDA output-radius transfer");
-        STEP(cudaStreamSynchronize(ctx->stream), "CUDA output completion");
-        // drain queued work before the caller may release its arrays
-        if (result != TPGP_CUDA_OK) cudaStreamSynchronize(ctx->stream);
-#undef STEP
-    }
-    code = cudaSetDevice(previous);
-    if (result == TPGP_CUDA_OK && code != cudaSuccess)
-        result = cuda_failure(code, "CUDA previous-device restoration", error, cap);
-    return result;
+    DeviceScope scope;
+    cudaError_t e = scope.enter(ctx->device);
+    if (e != cudaSuccess) return report.cuda(e, "device selection");
+    if ((e = ctx->scratch.reserve(Staging(plan).bytes)) != cudaSuccess)
+        return report.cuda(e, "staging allocation");
+    st = run_branch(plan, ctx->scratch.data(), ctx->sms, ctx->stream, keys, values, out_keys,
+                    out_values, out_radii, report);
+    e = scope.restore();
+    if (st == TPGP_CUDA_OK && e != cudaSuccess) return report.cuda(e, "restoring the caller's device");
+    return st;
 }
 
 // ---------------------------------------------------------------------------
@@ -356,18 +491,19 @@ extern "C" tpgp_cuda_status tpgp_cuda_branches(tpgp_cuda_context* ctx, const uin
 // Some callers cannot call cudaMalloc: code running inside a host allocator
 // or a signal-safe/real-time section, plugins whose host application owns
 // all device memory, or processes whose device memory is fully reserved by
-// another runtime.  For them the device staging buffers of the branch kernel
-// (input keys/values, output keys/values/radii, failure flag) live in one
-// file-scope array that the library's module brings with it; the call itself
-// allocates nothing.
+// another runtime.  For them the device staging of the branch kernel lives
+// in one file-scope array that the library's module brings with it; the
+// call itself allocates nothing.  The array's host-side name is not a device
+// address, so every call asks the runtime for the address on the selected
+// device (cheap once the module is loaded, and never stale after a device
+// reset reloaded the module elsewhere).
 namespace {
 
 constexpr size_t kStaticScratchBytes = size_t(16) << 20;  // 16 MiB per device
 static __device__ __align__(256) unsigned char g_branch_scratch[kStaticScratchBytes];
 
 constexpr int kMaxStaticDevices = 64;
-std::mutex g_static_lock;                                 // serializes every call
-void* g_static_address[kMaxStaticDevices] = {nullptr};    // device address, per device
+std::mutex g_static_lock;  // every call shares the array: calls are serialised
 
 }  // namespace
 
@@ -376,131 +512,48 @@ extern "C" tpgp_cuda_status tpgp_cuda_branches_static(
     size_t spins, size_t i, size_t j, unsigned qi, unsigned qj, double c, double s, double rc,
     double rs, int enclose, uint64_t* out_keys, double* out_values, double* out_radii,
     char* error, size_t cap) {
-    set_message(error, cap, "");
-    // the same argument checks, in the same order, as tpgp_cuda_branches
-    if (device_index < 0 || device_index >= kMaxStaticDevices || spins < 2 ||
-        words != spins / 32 + (spins % 32 != 0) || i >= spins || j >= spins || i == j ||
-        qi > 3 || qj > 3 || !std::isfinite(c) || !std::isfinite(s) || !std::isfinite(rc) ||
-        !std::isfinite(rs) || rc < 0 || rs < 0 || (enclose != 0 && enclose != 1)) {
-        set_message(error, cap,
-                    "Invalid CUDA branch device, dimensions, sites, generator, or trigonometric enclosure.");
-        return TPGP_CUDA_EINVAL;
-    }
-    if (!count) return TPGP_CUDA_OK;
-    size_t key_bytes, value_bytes, out_key_bytes, out_value_bytes, total, t;
-    if (!keys || !values || !out_keys || !out_values || !out_radii || !mul_ok(count, words, &t) ||
-        !mul_ok(t, sizeof(uint64_t), &key_bytes) || !mul_ok(count, sizeof(double), &value_bytes) ||
-        !mul_ok(key_bytes, 2, &out_key_bytes) || !mul_ok(value_bytes, 2, &out_value_bytes) ||
-        !mul_ok(key_bytes, 3, &total) || !mul_ok(value_bytes, 5, &t) || !add_ok(total, t, &total) ||
-        !add_ok(total, 128, &total)) {
-        set_message(error, cap, "Null CUDA array or packed-branch size overflow.");
-        return TPGP_CUDA_EINVAL;
-    }
-    if (total > kStaticScratchBytes) {
-        if (error && cap)
-            std::snprintf(error, cap,
-                          "Batch needs %zu bytes of staging; the allocation-free entry point holds "
-                          "at most %zu bytes ((24*n_words + 40) bytes per term). Split the batch.",
-                          total, kStaticScratchBytes);
-        return TPGP_CUDA_EINVAL;
-    }
-    const void* arrays[] = {keys, values, out_keys, out_values, out_radii};
-    const size_t lengths[] = {key_bytes, value_bytes, out_key_bytes, out_value_bytes,
-                              out_value_bytes};
-    for (int x = 0; x < 5; ++x)
-        for (int y = x + 1; y < 5; ++y)
-            if (ranges_overlap(arrays[x], lengths[x], arrays[y], lengths[y])) {
-                set_message(error, cap, "CUDA input/output arrays must be disjoint.");
-                return TPGP_CUDA_EINVAL;
-            }
+    Report report(error, cap);
+    if (device_index < 0 || device_index >= kMaxStaticDevices)
+        return report.fail(TPGP_CUDA_EINVAL, "tpgp_cuda: device index %d outside 0..%d",
+                           device_index, kMaxStaticDevices - 1);
+    if (!valid_geometry(words, spins, i, j, qi, qj, c, s, rc, rs, enclose))
+        return report.fail(TPGP_CUDA_EINVAL,
+                           "tpgp_cuda: invalid rotation (spins %zu, words %zu, sites %zu/%zu, "
+                           "labels %u/%u, factors or enclose flag)", spins, words, i, j, qi, qj);
+    if (count == 0) return TPGP_CUDA_OK;
+    BranchPlan plan;
+    plan.count = count, plan.words = words, plan.spins = spins, plan.i = i, plan.j = j;
+    plan.qi = qi, plan.qj = qj, plan.c = c, plan.s = s, plan.rc = rc, plan.rs = rs;
+    plan.enclose = enclose;
+    tpgp_cuda_status st = plan_arrays(plan, keys, values, out_keys, out_values, out_radii, report);
+    if (st != TPGP_CUDA_OK) return st;
+    const size_t need = Staging(plan).bytes;
+    if (need > kStaticScratchBytes)
+        return report.fail(TPGP_CUDA_EINVAL,
+                           "tpgp_cuda: %zu terms need %zu bytes of staging; the allocation-free "
+                           "entry point holds at most %zu bytes ((24*n_words + 40) bytes per "
+                           "term); split the batch", count, need, kStaticScratchBytes);
     std::lock_guard<std::mutex> guard(g_static_lock);
-    tpgp_cuda_status result = TPGP_CUDA_OK;
-    int previous = 0, count_dev = 0;
-    cudaError_t code = cudaGetDeviceCount(&count_dev);
-    if (code != cudaSuccess) return cuda_failure(code, "CUDA device discovery", error, cap);
-    if (device_index >= count_dev) {
-        set_message(error, cap, "Requested CUDA device index is unavailable.");
-        return TPGP_CUDA_EINVAL;
-    }
-    if ((code = cudaGetDevice(&previous)) != cudaSuccess)
-        return cuda_failure(code, "CUDA current-device query", error, cap);
-    if ((code = cudaSetDevice(device_index)) != cudaSuccess)
-        return cuda_failure(code, "CUDA device selection", error, cap);
-    // set-up, once per device, with that device current: the host-side name
-    // of the array is not a device address, so ask the runtime for it
-    if (!g_static_address[device_index]) {
-        void* ptr = nullptr;
-        code = cudaGetSymbolAddress(&ptr, g_branch_scratch);
-        if (code != cudaSuccess) {
-            result = cuda_failure(code, "CUDA static scratch address", error, cap);
-            cudaSetDevice(previous);
-            return result;
-        }
-        g_static_address[device_index] = ptr;
-    }
-    unsigned char* base = static_cast<unsigned char*>(g_static_address[device_index]);
-    auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
-    size_t off = 0;
-    uint64_t* d_out_keys = reinterpret_cast<uint64_t*>(base + off);
-    off = align16(off + out_key_bytes);
-    double* d_out_values = reinterpret_cast<double*>(base + off);
-    off = align16(off + out_value_bytes);
-    double* d_out_radii = reinterpret_cast<double*>(base + off);
-    off = align16(off + out_value_bytes);
-    uint64_t* d_keys = reinterpret_cast<uint64_t*>(base + off);
-    off = align16(off + key_bytes);
-    double* d_values = reinterpret_cast<double*>(base + off);
-    off = align16(off + value_bytes);
-    unsigned* d_failure = reinterpret_cast<unsigned*>(base + off);
-    unsigned failure = 0;
-#define STEP(call, what)                                                      \
-    do {                                                                      \
-        if (result == TPGP_CUDA_OK) {                                         \
-            code = (call);                                                    \
-            if (code != cudaSuccess) result = cuda_failure(code, what, error, cap); \
-        }                                                                     \
-    } while (0)
-    STEP(cudaMemcpy(d_keys, keys, key_bytes, cudaMemcpyHostToDevice), "CUDA input-key transfer");
-    STEP(cudaMemcpy(d_values, values, value_bytes, cudaMemcpyHostToDevice),
-         "CUDA input-coefficient transfer");
-    // the array keeps the previous call's contents: the failure flag must start at zero
-    STEP(cudaMemset(d_failure, 0, sizeof(unsigned)), "CUDA status reset");
-    if (result == TPGP_CUDA_OK) {
-        int sms = 1;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_index);
-        const size_t want = (count + 255) / 256, cap_blocks = (size_t)(sms > 0 ? sms : 1) * 16;
-        const unsigned blocks = (unsigned)(want < cap_blocks ? want : cap_blocks);
-        if (words == 1)
-            k_branch<1><<<blocks, 256>>>(d_keys, d_values, count, words, spins, i, j, qi, qj, c,
-                                         s, rc, rs, enclose, d_out_keys, d_out_values,
-                                         d_out_radii, d_failure);
-        else if (words == 2)
-            k_branch<2><<<blocks, 256>>>(d_keys, d_values, count, words, spins, i, j, qi, qj, c,
-                                         s, rc, rs, enclose, d_out_keys, d_out_values,
-                                         d_out_radii, d_failure);
-        else
-            k_branch<0><<<blocks, 256>>>(d_keys, d_values, count, words, spins, i, j, qi, qj, c,
-                                         s, rc, rs, enclose, d_out_keys, d_out_values,
-                                         d_out_radii, d_failure);
-        STEP(cudaGetLastError(), "CUDA branch-kernel launch");
-    }
-    STEP(cudaMemcpy(&failure, d_failure, sizeof(unsigned), cudaMemcpyDeviceToHost),
-         "CUDA branch-kernel execution");
-    if (result == TPGP_CUDA_OK && failure) {
-        result = (failure & 1u) ? TPGP_CUDA_EINVAL : TPGP_CUDA_ENUMERIC;
-        set_message(error, cap,
-                    (failure & 1u) ? "CUDA input keys contain nonzero padding bits."
-                                   : "CUDA branch arithmetic or coefficients are nonfinite.");
-    }
-    STEP(cudaMemcpy(out_keys, d_out_keys, out_key_bytes, cudaMemcpyDeviceToHost),
-         "CUDA output-key transfer");
-    STEP(cudaMemcpy(out_values, d_out_values, out_value_bytes, cudaMemcpyDeviceToHost),
-         "CUDA output-coefficient transfer");
-    STEP(cudaMemcpy(out_radii, d_out_radii, out_value_bytes, cudaMemcpyDeviceToHost),
-         "CUDA output-radius transfer");
-#undef STEP
-    code = cudaSetDevice(previous);
-    if (result == TPGP_CUDA_OK && code != cudaSuccess)
-        result = cuda_failure(code, "CUDA previous-device restoration", error, cap);
-    return result;
+    int devices = 0;
+    cudaError_t e = cudaGetDeviceCount(&devices);
+    if (e != cudaSuccess) return report.cuda(e, "device count");
+    if (device_index >= devices)
+        return report.fail(TPGP_CUDA_EINVAL, "tpgp_cuda: device %d requested, %d visible",
+                           device_index, devices);
+    DeviceScope scope;
+    if ((e = scope.enter(device_index)) != cudaSuccess) return report.cuda(e, "device selection");
+    void* base = nullptr;  // the array's address on this device
+    if ((e = cudaGetSymbolAddress(&base, g_branch_scratch)) != cudaSuccess)
+        return report.cuda(e, "static staging address lookup");
+    int sms = 1;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_index)) !=
+        cudaSuccess)
+        return report.cuda(e, "multiprocessor count");
+    // the legacy default stream: no stream to create; the array keeps the
+    // previous call's contents, and run_branch clears the failure flag
+    st = run_branch(plan, static_cast<unsigned char*>(base), sms, cudaStreamLegacy, keys, values,
+                    out_keys, out_values, out_radii, report);
+    e = scope.restore();
+    if (st == TPGP_CUDA_OK && e != cudaSuccess) return report.cuda(e, "restoring the caller's device");
+    return st;
 }

@@ -70,17 +70,21 @@ tpgp_cuda_status tpgp_cuda_branches(tpgp_cuda_context *context, const uint64_t *
  * device memory, processes whose device memory another runtime has reserved:
  * the device staging buffers live in a 16 MiB array that the library's
  * module holds on every GPU that loads it, until exit.  No context is
- * needed; device_index selects the GPU (the previous current device is
- * restored).  Arguments, slot order, statuses and outputs are those of
- * tpgp_cuda_branches; a batch whose staging exceeds the array,
- * (24*n_words + 40)*count + 128 bytes > 16 MiB, is rejected with EINVAL and a
- * message (split it).  The first call on a device looks up the array's
- * device address with that device current; make that first call before any
- * stream capture.  Every call on a device shares the array and keeps the
- * previous call's contents (the failure flag is cleared per call); calls
- * that overlapped on the GPU would race, so this entry point serializes its
- * callers with a process-wide lock and returns only after its copies
- * completed. */
+ * needed; device_index (0..63) selects the GPU and the caller's current
+ * device is restored.  Arguments, slot order, statuses and outputs are those
+ * of tpgp_cuda_branches; a batch whose staging exceeds the array,
+ * (24*n_words + 40)*count + 96 bytes > 16 MiB, is rejected with EINVAL and a
+ * message (split it).  Every call looks up the array's device address with
+ * that device current (after a device reset the module, and the array, may
+ * sit elsewhere); the first call on a device, and the first after a reset,
+ * loads the module, so make it before any stream capture.  The call runs on
+ * the legacy default stream: it waits for, and holds up, other work on that
+ * stream and on blocking streams of the process, and it cannot run while a
+ * global-mode stream capture is open on any thread.  Every call on a device
+ * shares the array and keeps the previous call's contents (the failure flag
+ * is cleared per call); calls that overlapped on the GPU would race, so this
+ * entry point serializes its callers with a process-wide lock and returns
+ * only after its copies completed. */
 tpgp_cuda_status tpgp_cuda_branches_static(int device_index, const uint64_t *keys,
                                            const double *values, size_t count, size_t n_words,
                                            size_t n_spins, size_t i, size_t j, unsigned qi,

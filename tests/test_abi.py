@@ -48,12 +48,12 @@ def test_argument_checks_need_no_device(lib):
     f = lib.tpgp_cuda_branches
     f.restype = C.c_int
     err = C.create_string_buffer(256)
-    # NULL context -> EINVAL before any CUDA call (engine/src/cuda_rev.cu:180-186)
+    # NULL context -> EINVAL before any CUDA call (the status of engine/src/cuda_rev.cu:180-186)
     st = f(None, None, None, C.c_size_t(0), C.c_size_t(1), C.c_size_t(2), C.c_size_t(0),
            C.c_size_t(1), C.c_uint(3), C.c_uint(3), C.c_double(.6), C.c_double(.8),
            C.c_double(0), C.c_double(0), C.c_int(1), None, None, None, err, C.c_size_t(256))
     assert st == 1
-    assert b"Invalid" in err.value
+    assert b"NULL context" in err.value
 
 
 def test_sm103a_code_in_library():

@@ -5,8 +5,9 @@ inside a host allocator or a real-time section, plugins whose host
 application owns all device memory): its staging buffers live in a static
 16 MiB device array instead of memory the library allocates.  Its outputs
 must equal tpgp_cuda_branches' bit for bit, on consecutive calls that share
-the array (so leftovers from one call must not leak into the next).  This
-file is collected last so a failure here never hides the other GPU tests.
+the array (so leftovers from one call must not leak into the next), and a
+run of calls must leave the device's free memory unchanged.  This file is
+collected last so a failure here never hides the other GPU tests.
 """
 import ctypes as C
 
@@ -105,3 +106,22 @@ def test_failure_flag_does_not_leak_and_limit_is_enforced(lib_ctx):
     keys, values, words = random_batch(22, big, 16)
     d = call(lib, True, ctx, keys, values, big, words, 16, 0, 1, 3, 3, .6, .8, 0, 0, 0)
     assert d[0] == 1 and "at most" in d[4]
+
+
+def test_static_calls_leave_free_memory_unchanged(lib_ctx):
+    """After a warm-up call (which loads the module and its array), a run of
+    allocation-free calls of several sizes changes the device's free memory
+    by nothing.  The ordinary entry point is kept out of the window."""
+    torch = pytest.importorskip("torch")
+    lib, _ = lib_ctx
+    keys, values, words = random_batch(31, 2000, 64)
+    assert call(lib, True, None, keys, values, 2000, words, 64, 0, 5, 1, 2, .6, .8, 0, 0, 0)[0] == 0
+    torch.cuda.synchronize(0)
+    free_before, _ = torch.cuda.mem_get_info(0)
+    for seed, count, spins in ((32, 100, 16), (33, 60000, 64), (34, 3000, 1000), (35, 1, 2)):
+        keys, values, words = random_batch(seed, count, spins)
+        st = call(lib, True, None, keys, values, count, words, spins, 0, 1, 3, 1, .28, .96, 0, 0,
+                  0)
+        assert st[0] == 0, st[4]
+    free_after, _ = torch.cuda.mem_get_info(0)
+    assert free_after == free_before
