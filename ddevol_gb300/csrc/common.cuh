@@ -345,6 +345,13 @@ struct DeviceState {
     unsigned long long rotations_done;      // rotations committed in the current call
     unsigned long long terms_in;            // input terms of the committed rotations
     Ledger ledger;
+    // the hash-table step's input and output map buffers, set per call, so
+    // one captured step serves whichever buffers hold the map
+    const uint64_t* in_keys;
+    const double* in_vals;
+    uint64_t* out_keys;
+    double* out_vals;
+    unsigned long long out_cap;
 };
 
 // --------------------------------------------------------- decoupled look-back

@@ -1,7 +1,7 @@
 // Sort-free Strang step for the bound ledger: the map lives in an
 // open-addressing hash table for the duration of one step, every rotation is
-// one pass over the table, and the map is sorted back into the reference
-// layout once per step.
+// one pass over the table's occupied slots, and the map is sorted back into
+// the reference layout once per step.
 //
 // Why it is exact.  A rotation by Q pairs every anticommuting key K with its
 // partner K xor Q (anticommutation with Q is invariant under multiplication
@@ -16,19 +16,25 @@
 // path uses, so keys, values and the bound ledger are bitwise those of the
 // sorted path.
 //
-// Table.  tags[s]: 0 empty, 1 present at step start, r+2 inserted by
-// rotation r.  Keys never leave the table during a step (a removed key keeps
-// its slot with value 0), so linear probing needs no tombstones: a present
-// key is always found before the first empty slot of its probe sequence.
-// Values are double-buffered per rotation (read vals[r&1], write
-// vals[(r+1)&1]); every occupied slot's new value is written exactly once
-// per rotation:
-//   commuting key                   -> its own thread
-//   pair with at least one live key -> the thread of the smaller live key
-//   pair with both keys dead        -> each key's own thread writes 0
-//   key inserted by this rotation   -> the inserting thread.
-// A key looked up in rotation r is never inserted by another thread in r
-// (only its partner inserts it), so probes may skip slots tagged r+2.
+// Table.  One record per slot -- the key, the value's bit pattern and a tag
+// (0 empty, 1 present at step start, k+2 inserted by pass k) -- 32 bytes for
+// one- and two-word keys (a single 32-byte load), 48 bytes for three and four
+// words.  Keys never leave the table during a step (a removed key keeps its
+// slot with value 0), so linear probing needs no tombstones: a present key is
+// always found before the first empty slot of its probe sequence.  Every
+// claimed slot is also appended to an occupied-slot list in claim order, and
+// a pass walks that list, so its threads see only occupied slots (whatever
+// the table's load) and a warp's lanes do the same kind of work.
+//
+// Values are updated in place.  The pair {K, K xor Q} is owned by its
+// smaller member among the keys present when the pass starts (dead keys,
+// value 0, included); ownership depends on keys and tags only, which no
+// thread changes during a pass, so exactly one thread reads and writes the
+// pair's two values, and a commuting key's value is touched by its own
+// thread only.  A dead member contributes no child: the owner combines the
+// live members exactly as the reference merges the children that exist.  A
+// key looked up in pass k is never inserted by another thread in k (only its
+// pair's owner inserts it), so probes skip slots tagged k+2.
 //
 // Ledger and limits.  Each rotation adds its born/died/removed counts and
 // fixed-point sums to per-rotation stat slots; k_hash_chain then applies,
@@ -45,37 +51,143 @@ constexpr int kHashBlock = 256;
 constexpr int kMaxProbe = 2048;  // linear-probe bound; hitting it reports ST_TABLE
 constexpr int kStatSlots = 32;   // stat slots per rotation (spreads the atomics)
 constexpr int kSortBlock = 256, kSortItems = 8, kSortTile = kSortBlock * kSortItems;
+constexpr uint32_t kNoSlot = 0xffffffffu;  // list entry reserved but not yet written
 
+// Per-rotation stat slot.  The removed-weight sums are 128-bit integers
+// accumulated as four 32-bit limbs, each summed in its own 64-bit counter by
+// reductions that return nothing (no CTA waits on an atomic's result);
+// k_hash_reduce recombines the limbs exactly (fewer than 2^32 addends per
+// counter).
 struct HashStat {
-    unsigned long long l1_lo, l1_hi, sq_lo, sq_hi;
+    unsigned long long l1[4], sq[4];
     unsigned long long born, died, removed;
     unsigned int flags, pad;
+    unsigned long long unused[4];
 };
-static_assert(sizeof(HashStat) == 64, "stat slot is one 64-byte line");
+static_assert(sizeof(HashStat) == 128, "stat slot is two 64-byte lines");
+
+// What a pass needs of its rotation, passed by value as a kernel parameter
+// (constant bank) so no thread waits on a global load for it.
+// anti / plus: bit 4 pi + pj is set when a key with symbols (pi, pj) at the
+// rotation's sites anticommutes with the generator / has a + sign on its
+// sin child (the phase table of engine/src/tpgp_rev.c:414-417); the
+// partner's index is the key's xor qmix = 4 qi + qj.
+// settled: 1 when every live value already passed this pass's threshold (a
+// later pass of a list with one threshold), so commuting keys, whose value
+// the rotation leaves unchanged, need no work at all.
+struct PassParams {
+    int i_word, i_shift, j_word, j_shift;
+    unsigned qi, qj;
+    unsigned anti, plus, qmix;
+    unsigned settled;
+    double c, s;
+    unsigned long long threshold_bits;
+    uint64_t mask[4];
+    int fx_unit1, fx_unit2;
+};
+
+__host__ __device__ inline PassParams pass_params(const RotParams& r) {
+    PassParams p;
+    p.i_word = r.i_word;
+    p.i_shift = r.i_shift;
+    p.j_word = r.j_word;
+    p.j_shift = r.j_shift;
+    p.qi = r.qi;
+    p.qj = r.qj;
+    p.anti = p.plus = 0u;
+    for (unsigned pi = 0; pi < 4; ++pi)
+        for (unsigned pj = 0; pj < 4; ++pj) {
+            const bool ai = r.qi && pi && r.qi != pi, aj = r.qj && pj && r.qj != pj;
+            const unsigned ei = ai ? ((r.qi % 3u) + 1u == pi ? 1u : 3u) : 0u;
+            const unsigned ej = aj ? ((r.qj % 3u) + 1u == pj ? 1u : 3u) : 0u;
+            if (ai != aj) p.anti |= 1u << (4 * pi + pj);
+            if (((ei + ej) & 3u) == 1u) p.plus |= 1u << (4 * pi + pj);
+        }
+    p.qmix = 4u * r.qi + r.qj;
+    p.settled = 0u;
+    p.c = r.c;
+    p.s = r.s;
+    p.threshold_bits = r.threshold_bits;
+    for (int w = 0; w < 4; ++w) p.mask[w] = r.mask[w];
+    p.fx_unit1 = r.fx_unit1;
+    p.fx_unit2 = r.fx_unit2;
+    return p;
+}
 
 struct HashArgs {
     const RotParams* ps;  // the step's rotation list (device)
     unsigned rotations;
     const uint2* runs;    // fused passes: (first rotation, count) per pass
     unsigned passes;      // kernels over the table (= rotations when not fused)
-    uint32_t* tags;
-    uint64_t* keys;                 // [S][W]
-    unsigned long long* vals[2];    // coefficient bit patterns, double-buffered
+    unsigned long long* rec;        // [S] records of rec_words<W>() words
+    unsigned long long* occ;        // occupied-slot list: entries of list_words<W>() words
     unsigned long long slots;       // S (any size: slots are h * S >> 64)
     HashStat* stats;                // [rotations][kStatSlots]
-    unsigned long long* claimed;    // slots claimed during the step
-    const uint64_t* in_keys;        // the step's input map (never written); its
-    const double* in_vals;          // length is st->n when the step starts
-    uint64_t* out_keys;             // the step's output map
-    double* out_vals;
-    unsigned long long out_cap;
+    unsigned long long* claimed;    // slots claimed during the step = entries of occ
     uint64_t* ek;                   // extraction / sort ping-pong buffers, S entries
     unsigned long long* ev;
     uint64_t* tk;
     unsigned long long* tv;
-    unsigned* hist;                 // [256][tiles] digit counts, then offsets
+    unsigned* hist;                 // radix sort: digit counts / offsets, look-back words
     DeviceState* st;
 };
+
+// Record layout: words 0..W-1 the key, word W the value bits, the low half
+// of word W+1 the tag.
+template <int W>
+__host__ __device__ constexpr int rec_words() {
+    return W <= 2 ? 4 : 6;
+}
+
+template <int W>
+struct Rec {
+    Key<W> key;
+    unsigned long long val;
+    uint32_t tag;
+};
+
+// One record in one access for W <= 2 (a 32-byte vector load, L2 only: the
+// persistent variant reads records other SMs wrote in the same launch).
+template <int W>
+__device__ __forceinline__ Rec<W> load_rec(const unsigned long long* rec, unsigned long long s) {
+    const unsigned long long* p = rec + s * rec_words<W>();
+    Rec<W> r;
+    if constexpr (W <= 2) {
+        unsigned long long x0, x1, x2, x3;
+        asm volatile("ld.global.cg.v4.u64 {%0, %1, %2, %3}, [%4];"
+                     : "=l"(x0), "=l"(x1), "=l"(x2), "=l"(x3)
+                     : "l"(p));
+        r.key.w[0] = x0;
+        if constexpr (W == 1) {
+            r.val = x1;
+            r.tag = (uint32_t)x2;
+        } else {
+            r.key.w[1] = x1;
+            r.val = x2;
+            r.tag = (uint32_t)x3;
+        }
+    } else {
+        const ulonglong2 a = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+        const ulonglong2 b = __ldcg(reinterpret_cast<const ulonglong2*>(p) + 1);
+        const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2*>(p) + 2);
+        const unsigned long long x[6] = {a.x, a.y, b.x, b.y, c.x, c.y};
+#pragma unroll
+        for (int w = 0; w < W; ++w) r.key.w[w] = x[w];
+        r.val = x[W];
+        r.tag = (uint32_t)x[W + 1];
+    }
+    return r;
+}
+
+template <int W>
+__device__ __forceinline__ uint32_t* rec_tag(unsigned long long* rec, unsigned long long s) {
+    return reinterpret_cast<uint32_t*>(rec + s * rec_words<W>() + W + 1);
+}
+template <int W>
+__device__ __forceinline__ void store_val(unsigned long long* rec, unsigned long long s,
+                                          unsigned long long bits) {
+    rec[s * rec_words<W>() + W] = bits;
+}
 
 __device__ __forceinline__ unsigned long long fmix64(unsigned long long h) {
     h ^= h >> 33;
@@ -115,40 +227,123 @@ __device__ __forceinline__ void pair_signs(const RotParams& p, uint64_t wi, uint
     plus_p = ((phase_exponent(p.qi, pi ^ p.qi) + phase_exponent(p.qj, pj ^ p.qj)) & 3u) == 1u;
 }
 
-// Slot of key k (tags other than `skip` compared), or -1 with *empty_at the
-// first empty slot of its probe sequence.  *overflow when the probe bound is hit.
+// Looks up key k from its first probe slot `s`, whose record `r` the caller
+// has already loaded: returns its slot (tags equal to `skip` ignored), or -1
+// with *empty_at the first empty slot of the probe sequence; *overflow when
+// the probe bound is hit.  *rv receives the found record's value.
 template <int W>
-__device__ __forceinline__ long long hash_find(const HashArgs& a, const Key<W>& k, uint32_t skip,
-                                               unsigned long long* empty_at, bool* overflow) {
-    unsigned long long s = slot_of(hash_of<W>(k), a.slots);
+__device__ __forceinline__ long long probe_from(const HashArgs& a, const Key<W>& k,
+                                                unsigned long long s, Rec<W> r, uint32_t skip,
+                                                unsigned long long* empty_at,
+                                                unsigned long long* rv, bool* overflow) {
     for (int i = 0; i < kMaxProbe; ++i) {
-        const uint32_t tag = __ldcg(a.tags + s);
-        if (tag == 0) {
+        if (r.tag == 0u) {
             *empty_at = s;
             return -1;
         }
-        if (tag != skip && key_eq<W>(load_key<W>(a.keys, s), k)) return (long long)s;
+        if (r.tag != skip && key_eq<W>(r.key, k)) {
+            *rv = r.val;
+            return (long long)s;
+        }
         s = next_slot(s, a.slots);
+        r = load_rec<W>(a.rec, s);
     }
     *overflow = true;
     return -1;
 }
 
-// Claims the first empty slot at or after `from` for k (tag `stamp`).
+// Claims the first empty slot at or after `from` for k (tag `stamp`) and
+// writes its key and value; the caller appends the slot to the list.
 template <int W>
 __device__ __forceinline__ long long hash_insert(const HashArgs& a, const Key<W>& k,
-                                                 unsigned long long from, uint32_t stamp,
-                                                 bool* overflow) {
+                                                 unsigned long long bits, unsigned long long from,
+                                                 uint32_t stamp, bool* overflow) {
     unsigned long long s = from;
     for (int i = 0; i < kMaxProbe; ++i) {
-        if (__ldcg(a.tags + s) == 0u && atomicCAS(a.tags + s, 0u, stamp) == 0u) {
-            store_key<W>(a.keys, s, k);
+        uint32_t* tag = rec_tag<W>(a.rec, s);
+        if (__ldcg(tag) == 0u && atomicCAS(tag, 0u, stamp) == 0u) {
+            unsigned long long* p = a.rec + s * rec_words<W>();
+#pragma unroll
+            for (int w = 0; w < W; ++w) p[w] = k.w[w];
+            p[W] = bits;
             return (long long)s;
         }
         s = next_slot(s, a.slots);
     }
     *overflow = true;
     return -1;
+}
+
+// Occupied-slot list entry: the key (words 0..W-1; keys never change during
+// a step, so a pass reads a key here and starts its partner probe without
+// first loading the slot's record) and, in word W, the slot (low half) and
+// the stamp of the pass that claimed it (high half), stored together so a
+// reader never sees one without the other.  An entry whose word W is all
+// ones (the list's fill) is reserved but not yet written.
+template <int W>
+__host__ __device__ constexpr int list_words() {
+    return W == 1 ? 2 : (W <= 3 ? 4 : 6);
+}
+constexpr unsigned long long kNoEntry = ~0ull;
+
+template <int W>
+struct Entry {
+    Key<W> key;
+    uint32_t slot, stamp;  // slot kNoSlot: not written yet
+};
+
+template <int W>
+__device__ __forceinline__ Entry<W> load_entry(const unsigned long long* occ, unsigned long long i) {
+    const unsigned long long* p = occ + i * list_words<W>();
+    Entry<W> e;
+    unsigned long long tail;
+    if constexpr (W == 1) {
+        const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+        e.key.w[0] = v.x;
+        tail = v.y;
+    } else if constexpr (W <= 3) {
+        unsigned long long x0, x1, x2, x3;
+        asm volatile("ld.global.cg.v4.u64 {%0, %1, %2, %3}, [%4];"
+                     : "=l"(x0), "=l"(x1), "=l"(x2), "=l"(x3)
+                     : "l"(p));
+        const unsigned long long x[4] = {x0, x1, x2, x3};
+#pragma unroll
+        for (int w = 0; w < W; ++w) e.key.w[w] = x[w];
+        tail = x[W];
+    } else {
+        const ulonglong2 a = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+        const ulonglong2 b = __ldcg(reinterpret_cast<const ulonglong2*>(p) + 1);
+        const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2*>(p) + 2);
+        e.key.w[0] = a.x;
+        e.key.w[1] = a.y;
+        e.key.w[2] = b.x;
+        e.key.w[3] = b.y;
+        tail = c.x;
+    }
+    e.slot = tail == kNoEntry ? kNoSlot : (uint32_t)tail;
+    e.stamp = (uint32_t)(tail >> 32);
+    return e;
+}
+
+template <int W>
+__device__ __forceinline__ void store_entry(unsigned long long* occ, unsigned long long i,
+                                            const Key<W>& k, unsigned long long slot, uint32_t stamp) {
+    unsigned long long* p = occ + i * list_words<W>();
+#pragma unroll
+    for (int w = 0; w < W; ++w) p[w] = k.w[w];
+    p[W] = (slot & 0xffffffffull) | ((unsigned long long)stamp << 32);
+}
+
+// Reserves list entries for the lanes with `want` set (one atomic per warp;
+// every lane of the warp calls it) and returns each such lane's index.
+__device__ __forceinline__ unsigned long long list_reserve(const HashArgs& a, bool want) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) return 0ull;
+    const unsigned lane = threadIdx.x & 31u, leader = (unsigned)(__ffs(m) - 1);
+    unsigned long long at = 0;
+    if (lane == leader) at = atomicAdd(a.claimed, (unsigned long long)__popc(m));
+    at = __shfl_sync(0xffffffffu, at, leader);
+    return at + __popc(m & lanemask_lt());
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x) {
@@ -170,33 +365,50 @@ __device__ __forceinline__ void atomic_add_u128(unsigned long long* lo, unsigned
 }
 
 // --------------------------------------------------------------- build
+// Inserts the step's input map (stamp 1).  Loops are warp-uniform so that
+// list_reserve's ballot sees every lane.
 template <int W>
 __global__ void __launch_bounds__(kHashBlock) k_hash_build(HashArgs a) {
     bool overflow = false;
-    unsigned long long claimed = 0;
     const unsigned long long n = __ldcg(&a.st->n);
+    // the step's input map (never written)
+    const uint64_t* in_keys = a.st->in_keys;
+    const double* in_vals = a.st->in_vals;
+    const unsigned lane = threadIdx.x & 31u;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += stride) {
-        const Key<W> key = load_key<W>(a.in_keys, k);
-        const long long s = hash_insert<W>(a, key, slot_of(hash_of<W>(key), a.slots), 1u, &overflow);
-        if (s >= 0) {
-            a.vals[0][s] = dbits(__ldcg(a.in_vals + k));
-            ++claimed;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+         base < n; base += stride) {
+        const unsigned long long k = base + lane;
+        long long s = -1;
+        Key<W> key;
+        if (k < n) {
+            key = load_key<W>(in_keys, k);
+            const unsigned long long bits = dbits(__ldcg(in_vals + k));
+            s = hash_insert<W>(a, key, bits, slot_of(hash_of<W>(key), a.slots), 1u, &overflow);
         }
+        const unsigned long long at = list_reserve(a, s >= 0);
+        if (s >= 0) store_entry<W>(a.occ, at, key, (unsigned long long)s, 1u);
     }
-    claimed = warp_sum_u64(claimed);
-    if ((threadIdx.x & 31) == 0 && claimed) atomicAdd(a.claimed, claimed);
     if (overflow) atomicOr(&a.st->status, ST_TABLE);
 }
 
 // --------------------------------------------------------------- rotation
-// Per-thread counts (32-bit: a thread handles far fewer than 2^32 slots);
-// the removed-weight sums go straight into the CTA's shared 128-bit
-// accumulators, which keeps them out of the probe loop's registers.
+// Per-thread counts (32-bit: a thread handles far fewer than 2^32 slots)
+// and removed-weight sums (exact 128-bit fixed point), reduced per warp by
+// shuffles and per CTA once at the end of a pass, so no thread waits on a
+// shared or global atomic while it removes terms.
 struct PairTally {
-    unsigned born, died, removed, claimed, flags;
+    unsigned born, died, removed, flags;
+    U128 l1, sq;
 };
+
+__device__ __forceinline__ PairTally empty_tally() {
+    PairTally t;
+    t.born = t.died = t.removed = t.flags = 0u;
+    t.l1 = U128{0ull, 0ull};
+    t.sq = U128{0ull, 0ull};
+    return t;
+}
 
 // Exact 128-bit accumulation into shared memory under concurrent adders.
 __device__ __forceinline__ void shared_add_u128(unsigned long long* acc, const U128& x) {
@@ -210,12 +422,10 @@ __device__ __forceinline__ void shared_add_u128(unsigned long long* acc, const U
 
 // New value of one key of a pair: exact zero -> dropped; |x| <= threshold
 // (identity exempt) -> removed into the fixed-point sums; else kept.
-// Returns the bit pattern to store (0 when dropped or removed).  acc: the
-// CTA's shared (l1 lo, l1 hi, sq lo, sq hi).
-template <int W>
-__device__ __forceinline__ unsigned long long settle(const RotParams& p, const Key<W>& key,
-                                                     double x, bool was_live, PairTally& t,
-                                                     unsigned long long* acc) {
+// Returns the bit pattern to store (0 when dropped or removed).
+template <int W, typename P>
+__device__ __forceinline__ unsigned long long settle(const P& p, const Key<W>& key,
+                                                     double x, bool was_live, PairTally& t) {
     if (!is_finite(x)) t.flags |= ST_NUMERIC;
     unsigned long long out = dbits(x);
     if (is_zero(x)) {
@@ -223,8 +433,8 @@ __device__ __forceinline__ unsigned long long settle(const RotParams& p, const K
     } else if (!key_is_zero<W>(key) && abs_bits(x) <= p.threshold_bits) {
         U128 x1, x2;
         fixed_terms(x, p.fx_unit1, p.fx_unit2, x1, x2);
-        shared_add_u128(acc, x1);
-        shared_add_u128(acc + 2, x2);
+        u128_add(t.l1, x1);
+        u128_add(t.sq, x2);
         ++t.removed;
         out = 0;
     }
@@ -233,170 +443,269 @@ __device__ __forceinline__ unsigned long long settle(const RotParams& p, const K
     return out;
 }
 
-// One rotation over the table (one CTA's share of the slots): each slot's
-// tag, value and key are loaded in one round trip, and an anticommuting
-// key's first probe loads the probe slot's tag, key and value together.
-template <int W, int NT>
-__device__ __forceinline__ void hash_pass(const HashArgs& a, unsigned r, unsigned k) {
-    constexpr int U = 1;
-    __shared__ PairTally s_t[NT / 32];
-    __shared__ unsigned long long s_acc[4];  // removed l1 (lo, hi), sq (lo, hi)
-    if (threadIdx.x < 4) s_acc[threadIdx.x] = 0ull;
-    __syncthreads();
-    const RotParams& p = a.ps[r];
-    const uint32_t stamp = k + 2u;  // pass k: stamps and buffers; rotation r: parameters
-    const unsigned long long* vin = a.vals[k & 1u];
-    unsigned long long* vout = a.vals[(k + 1u) & 1u];
-    const Key<W> Q = mask_key<W>(p);
-    const double c = p.c, s = p.s;
-    PairTally t;
-    t.born = t.died = t.removed = t.claimed = 0;
-    t.flags = 0;
-    const unsigned long long S = a.slots;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-         base < S; base += U * stride) {
-        // 1. own slots: tag, value and key loaded together
-        uint32_t tag[U];
-        unsigned long long vb[U];
-        Key<W> K[U];
+// Adds a 128-bit value into four 64-bit limb counters (no return values).
+__device__ __forceinline__ void red_add_limbs(unsigned long long* c, const U128& x) {
+    const unsigned long long l[4] = {x.lo & 0xffffffffull, x.lo >> 32, x.hi & 0xffffffffull,
+                                     x.hi >> 32};
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const unsigned long long slot = base + u * stride;
-            tag[u] = 0u;
-            vb[u] = 0ull;
-            if (slot < S) {
-                tag[u] = __ldcg(a.tags + slot);
-                vb[u] = __ldcg(vin + slot);
-                K[u] = load_key<W>(a.keys, slot);
-            }
-        }
-        // 2. classify; anticommuting keys start their partner probe, again
-        //    loading tag, key and value of the probe slot together
-        bool act[U], plus_k[U];
-        Key<W> P[U], PK[U];
-        unsigned long long ps[U], pv[U];
-        uint32_t pt[U];
+    for (int q = 0; q < 4; ++q)
+        if (l[q]) atomicAdd(c + q, l[q]);
+}
+// The limb counters' exact 128-bit total.
+__device__ __forceinline__ U128 limbs_total(const unsigned long long (&c)[4]) {
+    U128 t{c[0], 0ull};
+    u128_add(t, U128{c[1] << 32, c[1] >> 32});
+    u128_add(t, U128{0ull, c[2]});
+    u128_add(t, U128{0ull, c[3] << 32});
+    return t;
+}
+
+// Block totals of a pass, then one set of reductions into rotation r's stat slot.
+// Warp total of a 128-bit sum: sixteen-bit limbs summed by warp reductions
+// (each limb total stays below 2^21) and recombined exactly.
+__device__ __forceinline__ U128 warp_sum_u128(const U128& x) {
+    U128 t{0ull, 0ull};
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const unsigned long long slot = base + u * stride;
-            act[u] = false;
-            if (tag[u] == 0u || tag[u] >= stamp) continue;  // empty, or inserted by this rotation
-            bool anti;
-            branch_info(p, word_at<W>(K[u], p.i_word), word_at<W>(K[u], p.j_word), anti, plus_k[u]);
-            if (!anti) {
-                // commuting: merged value v + 0 = v, still subject to the
-                // threshold like every merged term (no anticommuting key pairs with it)
-                vout[slot] = vb[u] ? settle<W>(p, K[u], from_bits(vb[u]), true, t, s_acc) : 0ull;
-                continue;
-            }
-            act[u] = true;
-            P[u] = key_xor<W>(K[u], Q);
-            ps[u] = slot_of(hash_of<W>(P[u]), a.slots);
-            pt[u] = __ldcg(a.tags + ps[u]);
-            PK[u] = load_key<W>(a.keys, ps[u]);
-            pv[u] = __ldcg(vin + ps[u]);
+    for (int q = 0; q < 8; ++q) {
+        const unsigned long long word = q < 4 ? x.lo : x.hi;
+        const unsigned limb = (unsigned)(word >> (16 * (q & 3))) & 0xffffu;
+        const unsigned long long sum = __reduce_add_sync(0xffffffffu, limb);
+        const int sh = 16 * q;
+        U128 part;
+        if (sh < 64) {
+            part.lo = sum << sh;
+            part.hi = sh ? (sum >> (64 - sh)) : 0ull;
+        } else {
+            part.lo = 0ull;
+            part.hi = sum << (sh - 64);
         }
-        // 3. finish each probe and update the pair
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            if (!act[u]) continue;
-            const unsigned long long slot = base + u * stride;
-            long long found = -1;
-            unsigned long long empty_at = 0, pb = 0;
-            bool overflow = true;
-            for (int i = 0; i < kMaxProbe; ++i) {
-                if (pt[u] == 0u) {
-                    empty_at = ps[u];
-                    overflow = false;
-                    break;
-                }
-                if (pt[u] != stamp && key_eq<W>(PK[u], P[u])) {
-                    found = (long long)ps[u];
-                    pb = pv[u];
-                    overflow = false;
-                    break;
-                }
-                ps[u] = next_slot(ps[u], a.slots);
-                pt[u] = __ldcg(a.tags + ps[u]);
-                PK[u] = load_key<W>(a.keys, ps[u]);
-                pv[u] = __ldcg(vin + ps[u]);
-            }
-            if (overflow) {
-                t.flags |= ST_TABLE;
-                continue;
-            }
-            const bool k_live = vb[u] != 0ull, p_live = pb != 0ull;
-            if (!k_live) {
-                if (!p_live) vout[slot] = 0ull;  // both dead; the partner's thread clears its own
-                continue;                        // else the live partner updates the pair
-            }
-            if (p_live && key_less<W>(P[u], K[u])) continue;  // the smaller live key updates the pair
-            bool anti_p, plus_p;
-            branch_info(p, word_at<W>(P[u], p.i_word), word_at<W>(P[u], p.j_word), anti_p, plus_p);
-            const double v = from_bits(vb[u]);
-            double sk = __dmul_rn(v, s);  // K's sin child, landing on P
-            if (!plus_k[u]) sk = negate(sk);
-            double nk = __dmul_rn(v, c), np = sk;
-            if (p_live) {
-                const double vp = from_bits(pb);
-                double sp = __dmul_rn(vp, s);  // P's sin child, landing on K
-                if (!plus_p) sp = negate(sp);
-                nk = __dadd_rn(nk, sp);
-                np = __dadd_rn(__dmul_rn(vp, c), sk);
-            }
-            vout[slot] = settle<W>(p, K[u], nk, true, t, s_acc);
-            const unsigned long long pbits = settle<W>(p, P[u], np, p_live, t, s_acc);
-            if (found >= 0) {
-                vout[found] = pbits;
-            } else if (pbits) {
-                bool ovf = false;
-                const long long ns = hash_insert<W>(a, P[u], empty_at, stamp, &ovf);
-                if (ns >= 0) {
-                    vout[ns] = pbits;
-                    ++t.claimed;
-                } else {
-                    t.flags |= ST_TABLE;
-                }
-            }
-        }
+        u128_add(t, part);
     }
-    // block totals, then one set of atomics into this rotation's stat slot
+    return t;
+}
+
+// Warp total of a tally (every lane holds it; all lanes must call).
+__device__ __forceinline__ void warp_tally(PairTally& t) {
+    t.born = __reduce_add_sync(0xffffffffu, t.born);
+    t.died = __reduce_add_sync(0xffffffffu, t.died);
+    t.flags = __reduce_or_sync(0xffffffffu, t.flags);
+    if (__any_sync(0xffffffffu, t.removed != 0u)) {
+        t.removed = __reduce_add_sync(0xffffffffu, t.removed);
+        t.l1 = warp_sum_u128(t.l1);
+        t.sq = warp_sum_u128(t.sq);
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void flush_tally(const HashArgs& a, unsigned r, PairTally t,
+                                            PairTally* s_t) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        t.born += __shfl_down_sync(0xffffffffu, t.born, off);
-        t.died += __shfl_down_sync(0xffffffffu, t.died, off);
-        t.removed += __shfl_down_sync(0xffffffffu, t.removed, off);
-        t.claimed += __shfl_down_sync(0xffffffffu, t.claimed, off);
-        t.flags |= __shfl_down_sync(0xffffffffu, t.flags, off);
-    }
+    warp_tally(t);
     if (lane == 0) s_t[warp] = t;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long born = 0, died = 0, removed = 0, claimed = 0;
+        unsigned long long born = 0, died = 0, removed = 0;
         unsigned flags = 0;
+        U128 l1{0ull, 0ull}, sq{0ull, 0ull};
         for (int w = 0; w < NT / 32; ++w) {
             born += s_t[w].born;
             died += s_t[w].died;
             removed += s_t[w].removed;
-            claimed += s_t[w].claimed;
             flags |= s_t[w].flags;
+            u128_add(l1, s_t[w].l1);
+            u128_add(sq, s_t[w].sq);
         }
         HashStat* hs = a.stats + (size_t)r * kStatSlots + (blockIdx.x % kStatSlots);
-        atomic_add_u128(&hs->l1_lo, &hs->l1_hi, U128{s_acc[0], s_acc[1]});
-        atomic_add_u128(&hs->sq_lo, &hs->sq_hi, U128{s_acc[2], s_acc[3]});
+        red_add_limbs(hs->l1, l1);
+        red_add_limbs(hs->sq, sq);
         if (born) atomicAdd(&hs->born, born);
         if (died) atomicAdd(&hs->died, died);
         if (removed) atomicAdd(&hs->removed, removed);
-        if (claimed) atomicAdd(a.claimed, claimed);
         if (flags) atomicOr(&hs->flags, flags);
     }
 }
 
+// Index 4 pi + pj of a key's two site symbols in the pass's branch tables.
 template <int W>
-__global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, unsigned r, unsigned k) {
-    hash_pass<W, kHashBlock>(a, r, k);
+__device__ __forceinline__ unsigned pass_index(const PassParams& p, const Key<W>& k) {
+    const unsigned pi = site_symbol(word_at<W>(k, p.i_word), p.i_shift);
+    const unsigned pj = site_symbol(word_at<W>(k, p.j_word), p.j_shift);
+    return 4u * pi + pj;
+}
+
+// One rotation over the occupied slots, in rounds of NT list entries per
+// CTA.  Phase 1: every thread reads one list entry (key, slot, stamp) and
+// classifies the key; a commuting key needs no work once every value has
+// passed the threshold (else its value is re-thresholded in place), and an
+// anticommuting key (typically a small fraction) is queued in shared memory.
+// Phase 2: the queued keys, packed into the first warps, each load their
+// slot's record and the partner's first probe record at once, and the
+// pair's owner updates it.  Entries appended during the pass (this pass's
+// stamp, or not yet written) are skipped.  Inserts reserve their list
+// entries with one warp atomic issued together with their slot claims.
+//
+// The first round's entries are loaded without waiting for the list length:
+// entries past the length are unwritten (the list starts filled with all
+// ones), and entries appended by this pass carry this pass's stamp.
+template <int W, int NT>
+__device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p, unsigned r,
+                                          unsigned k) {
+    __shared__ PairTally s_t[NT / 32];
+    __shared__ Key<W> s_key[NT];
+    __shared__ uint32_t s_slot[NT];
+    __shared__ unsigned char s_idx[NT];
+    __shared__ unsigned s_n;
+    __shared__ unsigned long long s_len;
+    const uint32_t stamp = k + 2u;  // pass k: stamps; rotation r: parameters
+    Key<W> Q;
+#pragma unroll
+    for (int w = 0; w < W; ++w) Q.w[w] = p.mask[w];
+    const double c = p.c, s = p.s;
+    PairTally t = empty_tally();
+    const unsigned long long S = a.slots;  // also the list's capacity
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned long long stride = (unsigned long long)gridDim.x * NT;
+    unsigned long long base = (unsigned long long)blockIdx.x * NT;
+    Entry<W> E;
+    E.slot = kNoSlot;
+    E.stamp = 0u;
+    if (base + threadIdx.x < S) E = load_entry<W>(a.occ, base + threadIdx.x);
+    if (threadIdx.x == 0) {
+        s_len = min(__ldcg(a.claimed), S);
+        s_n = 0u;
+    }
+    for (;;) {
+        // ---- phase 1: classify, queue the anticommuting keys
+        bool anti = false;
+        unsigned idx = 0;
+        if (E.slot != kNoSlot && E.stamp < stamp) {
+            idx = pass_index<W>(p, E.key);
+            anti = (p.anti >> idx) & 1u;
+            if (!anti && !p.settled) {
+                // commuting: merged value v + 0 = v, still subject to the
+                // threshold like every merged term (no anticommuting key pairs with it)
+                const unsigned long long v = load_rec<W>(a.rec, E.slot).val;
+                if (v) {
+                    const unsigned long long out = settle<W>(p, E.key, from_bits(v), true, t);
+                    if (out != v) store_val<W>(a.rec, E.slot, out);
+                }
+            }
+        }
+        __syncthreads();  // s_n = 0 and s_len visible; the previous round's queue consumed
+        const unsigned m = __ballot_sync(0xffffffffu, anti);
+        if (m) {
+            const unsigned leader = (unsigned)(__ffs(m) - 1);
+            unsigned at = 0;
+            if (lane == leader) at = atomicAdd(&s_n, (unsigned)__popc(m));
+            at = __shfl_sync(0xffffffffu, at, leader) + __popc(m & lanemask_lt());
+            if (anti) {
+                s_key[at] = E.key;
+                s_slot[at] = E.slot;
+                s_idx[at] = (unsigned char)idx;
+            }
+        }
+        __syncthreads();
+        const unsigned n = s_n;
+        const unsigned long long len = s_len;
+        // ---- phase 2: the queued keys, one per thread of the first warps
+        if (warp * 32u < n) {
+            const unsigned q = warp * 32u + lane;
+            bool want = false;  // this lane inserts its partner P with value pbits at empty_at
+            Key<W> P;
+            unsigned long long pbits = 0, empty_at = 0;
+            if (q < n) {
+                const Key<W> K = s_key[q];
+                const unsigned long long slot = s_slot[q];
+                const unsigned qidx = s_idx[q];
+                P = key_xor<W>(K, Q);
+                const unsigned long long ps = slot_of(hash_of<W>(P), S);
+                const Rec<W> R = load_rec<W>(a.rec, slot);
+                unsigned long long pb = 0;
+                bool overflow = false;
+                const long long found =
+                    probe_from<W>(a, P, ps, load_rec<W>(a.rec, ps), stamp, &empty_at, &pb, &overflow);
+                if (overflow) {
+                    t.flags |= ST_TABLE;
+                } else if ((found < 0 || key_less<W>(K, P)) && (R.val | pb)) {
+                    // this thread owns the pair, and at least one member is live
+                    const bool k_live = R.val != 0ull, p_live = pb != 0ull;
+                    const bool plus_k = (p.plus >> qidx) & 1u;
+                    const bool plus_p = (p.plus >> (qidx ^ p.qmix)) & 1u;
+                    double nk, np;
+                    if (k_live) {
+                        const double v = from_bits(R.val);
+                        double sk = __dmul_rn(v, s);  // K's sin child, landing on P
+                        if (!plus_k) sk = negate(sk);
+                        nk = __dmul_rn(v, c);
+                        np = sk;
+                        if (p_live) {
+                            const double vp = from_bits(pb);
+                            double sp = __dmul_rn(vp, s);  // P's sin child, landing on K
+                            if (!plus_p) sp = negate(sp);
+                            nk = __dadd_rn(nk, sp);
+                            np = __dadd_rn(__dmul_rn(vp, c), sk);
+                        }
+                    } else {
+                        const double vp = from_bits(pb);
+                        double sp = __dmul_rn(vp, s);
+                        if (!plus_p) sp = negate(sp);
+                        nk = sp;
+                        np = __dmul_rn(vp, c);
+                    }
+                    const unsigned long long kbits = settle<W>(p, K, nk, k_live, t);
+                    pbits = settle<W>(p, P, np, p_live, t);
+                    if (kbits != R.val) store_val<W>(a.rec, slot, kbits);
+                    if (found >= 0) {
+                        if (pbits != pb) store_val<W>(a.rec, (unsigned long long)found, pbits);
+                    } else {
+                        want = pbits != 0ull;
+                    }
+                }
+            }
+            // inserts: the warp's list reservation and the lanes' slot claims in flight together
+            const unsigned mi = __ballot_sync(0xffffffffu, want);
+            if (mi) {
+                const unsigned leader = (unsigned)(__ffs(mi) - 1);
+                unsigned long long at = 0;
+                uint32_t old = 1u;
+                if (lane == leader) at = atomicAdd(a.claimed, (unsigned long long)__popc(mi));
+                if (want) old = atomicCAS(rec_tag<W>(a.rec, empty_at), 0u, stamp);
+                at = __shfl_sync(0xffffffffu, at, leader) + __popc(mi & lanemask_lt());
+                if (want) {
+                    long long ns = -1;
+                    if (old == 0u) {
+                        unsigned long long* d = a.rec + empty_at * rec_words<W>();
+#pragma unroll
+                        for (int w = 0; w < W; ++w) d[w] = P.w[w];
+                        d[W] = pbits;
+                        ns = (long long)empty_at;
+                    } else {  // another insert took the slot: the next empty one
+                        bool ovf = false;
+                        ns = hash_insert<W>(a, P, pbits, next_slot(empty_at, S), stamp, &ovf);
+                    }
+                    if (ns >= 0 && at < S) store_entry<W>(a.occ, at, P, (unsigned long long)ns, stamp);
+                    else t.flags |= ST_TABLE;
+                }
+            }
+        }
+        base += stride;  // block-uniform
+        if (base >= len) break;
+        E.slot = kNoSlot;
+        if (base + threadIdx.x < len) E = load_entry<W>(a.occ, base + threadIdx.x);
+        __syncthreads();  // every thread has read s_n before it is cleared
+        if (threadIdx.x == 0) s_n = 0u;
+    }
+    flush_tally<NT>(a, r, t, s_t);
+}
+
+// Launched with programmatic stream serialization (hash_pdl), a pass's CTAs
+// become resident while the previous pass drains and wait here for its
+// completion and memory; launched plainly, pdl_enter returns at once.
+template <int W>
+__global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, PassParams p, unsigned r,
+                                                               unsigned k) {
+    pdl_enter();
+    hash_pass<W, kHashBlock>(a, p, r, k);
 }
 
 // All rotations of a step in one cooperative launch (one CTA of 1024 threads
@@ -406,7 +715,7 @@ constexpr int kHashPersistentBlock = 1024;
 template <int W>
 __global__ void __launch_bounds__(kHashPersistentBlock, 1) k_hash_rotate_all(HashArgs a) {
     for (unsigned r = 0; r < a.rotations; ++r) {
-        hash_pass<W, kHashPersistentBlock>(a, r, r);
+        hash_pass<W, kHashPersistentBlock>(a, pass_params(a.ps[r]), r, r);
         if (!grid_barrier(a.st)) return;
     }
 }
@@ -416,13 +725,12 @@ __global__ void __launch_bounds__(kHashPersistentBlock, 1) k_hash_rotate_all(Has
 // XX, YY; six at the middle of a Strang step) whose generators span a group
 // G of at most four XOR patterns G = {0, b1, b2, b1 ^ b2}.  Every key's coset
 // K xor G is closed under each rotation of the run, so each coset is evolved
-// on its own through the whole run — per rotation exactly the pair rule of
+// on its own through the whole run -- per rotation exactly the pair rule of
 // hash_pass (commuting members keep v + 0, anticommuting members combine
 // with their partner a ^ label(Q)), with the zero drop, threshold and
-// removed-weight sums of that rotation — and only the final values are
-// written.  The smallest live member's thread evolves a coset; a coset with
-// no live member has each member's own thread clear its slot.  Results are
-// those of the run's rotations one by one.
+// removed-weight sums of that rotation -- and only the final values are
+// written.  The coset is owned by its smallest member present when the pass
+// starts; results are those of the run's rotations one by one.
 constexpr int kMaxRun = 6;
 
 template <int W>
@@ -435,19 +743,14 @@ template <int W>
 __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned k) {
     __shared__ unsigned long long s_acc[kMaxRun][4];
     __shared__ unsigned s_cnt[kMaxRun][3];  // born, died, removed
-    __shared__ unsigned s_claimed, s_flags;
+    __shared__ unsigned s_flags;
     for (int q = threadIdx.x; q < kMaxRun * 4; q += blockDim.x) (&s_acc[0][0])[q] = 0ull;
     for (int q = threadIdx.x; q < kMaxRun * 3; q += blockDim.x) (&s_cnt[0][0])[q] = 0u;
-    if (threadIdx.x == 0) {
-        s_claimed = 0u;
-        s_flags = 0u;
-    }
+    if (threadIdx.x == 0) s_flags = 0u;
     __syncthreads();
     const uint2 run = a.runs[k];
     const unsigned r0 = run.x, L = run.y;
     const uint32_t stamp = k + 2u;
-    const unsigned long long* vin = a.vals[k & 1u];
-    unsigned long long* vout = a.vals[(k + 1u) & 1u];
     // the run's group: G[1] = the first mask, G[2] the first other mask
     Key<W> G[4];
 #pragma unroll
@@ -464,158 +767,158 @@ __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned
     }
     G[3] = key_xor<W>(G[1], G[2]);
     const int gs = has_b2 ? 4 : 2;
-    unsigned flags = 0u, claimed = 0u;
+    unsigned flags = 0u;
     const unsigned long long S = a.slots;
+    const unsigned long long len = min(__ldcg(a.claimed), S);
+    const unsigned lane = threadIdx.x & 31u;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long slot = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-         slot < S; slot += stride) {
-        const uint32_t tag = __ldcg(a.tags + slot);
-        const unsigned long long vb = __ldcg(vin + slot);
-        const Key<W> K = load_key<W>(a.keys, slot);
-        if (tag == 0u || tag >= stamp) continue;  // empty, or inserted by this pass
-        // the coset's other members: first probe slots loaded together
-        Key<W> M[4], PK[4];
-        unsigned long long ps[4], pv[4], ea[4], v[4];
-        uint32_t pt[4];
-        long long sl[4];
-        M[0] = K;
-        sl[0] = (long long)slot;
-        v[0] = vb;
-        ea[0] = 0ull;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+         base < len; base += stride) {
+        const unsigned long long i = base + lane;
+        // a coset inserts at most three members: appended after the work
+        bool ins[4] = {false, false, false, false};
+        unsigned long long ins_slot[4] = {0, 0, 0, 0};
+        Key<W> ins_key[4];
+        Entry<W> E;
+        E.slot = kNoSlot;
+        E.stamp = stamp;
+        if (i < len) E = load_entry<W>(a.occ, i);
+        const uint32_t slot = E.slot;
+        Rec<W> R;
+        R.tag = stamp;
+        if (slot != kNoSlot && E.stamp < stamp) R = load_rec<W>(a.rec, slot);
+        if (R.tag < stamp) {
+            // the coset's other members: first probe records loaded together
+            Key<W> M[4];
+            Rec<W> PR[4];
+            unsigned long long ps[4], ea[4], v[4];
+            long long sl[4];
+            M[0] = R.key;
+            sl[0] = (long long)slot;
+            v[0] = R.val;
+            ea[0] = 0ull;
 #pragma unroll
-        for (int m = 1; m < 4; ++m) {
-            M[m] = key_xor<W>(K, G[m]);
-            sl[m] = -1;
-            v[m] = 0ull;
-            ea[m] = 0ull;
-            if (m < gs) {
-                ps[m] = slot_of(hash_of<W>(M[m]), S);
-                pt[m] = __ldcg(a.tags + ps[m]);
-                PK[m] = load_key<W>(a.keys, ps[m]);
-                pv[m] = __ldcg(vin + ps[m]);
-            }
-        }
-        bool overflow = false;
-#pragma unroll
-        for (int m = 1; m < 4; ++m) {
-            if (m >= gs) continue;
-            bool done = false;
-            for (int i = 0; i < kMaxProbe; ++i) {
-                if (pt[m] == 0u) {
-                    ea[m] = ps[m];
-                    done = true;
-                    break;
+            for (int m = 1; m < 4; ++m) {
+                M[m] = key_xor<W>(R.key, G[m]);
+                sl[m] = -1;
+                v[m] = 0ull;
+                ea[m] = 0ull;
+                if (m < gs) {
+                    ps[m] = slot_of(hash_of<W>(M[m]), S);
+                    PR[m] = load_rec<W>(a.rec, ps[m]);
                 }
-                if (pt[m] != stamp && key_eq<W>(PK[m], M[m])) {
-                    sl[m] = (long long)ps[m];
-                    v[m] = pv[m];
-                    done = true;
-                    break;
-                }
-                ps[m] = next_slot(ps[m], S);
-                pt[m] = __ldcg(a.tags + ps[m]);
-                PK[m] = load_key<W>(a.keys, ps[m]);
-                pv[m] = __ldcg(vin + ps[m]);
             }
-            if (!done) overflow = true;
-        }
-        if (overflow) {
-            flags |= ST_TABLE;
-            continue;
-        }
-        // the smallest live member evolves the coset
-        int h = -1;
+            bool overflow = false;
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-            if (m < gs && v[m] && (h < 0 || key_less<W>(M[m], pick<4, Key<W>>(M, h)))) h = m;
-        if (h < 0) {
-            vout[slot] = 0ull;  // no live member: each member clears its own slot
-            continue;
-        }
-        if (h != 0) continue;
-        double x[4];
-        bool live[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            live[m] = v[m] != 0ull;
-            x[m] = from_bits(v[m]);
-        }
-        for (unsigned l = 0; l < L; ++l) {
-            const RotParams& p = a.ps[r0 + l];
-            const Key<W> q = mask_key<W>(p);
-            const int b = key_eq<W>(q, G[1]) ? 1 : (key_eq<W>(q, G[2]) ? 2 : 3);
-            const double c = p.c, s = p.s;
-            bool anti[4], plus[4];
-#pragma unroll
-            for (int m = 0; m < 4; ++m) coset_sign<W>(p, M[m], anti[m], plus[m]);
-            double nx[4];
-            bool touched[4];
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                nx[m] = 0.0;
-                touched[m] = false;
+            for (int m = 1; m < 4; ++m) {
                 if (m >= gs) continue;
-                if (!anti[m]) {
-                    nx[m] = x[m];
-                    touched[m] = live[m];
-                    continue;
-                }
-                const int pb = m ^ b;
-                const bool lp = pick<4, bool>(live, pb);
-                double sp = __dmul_rn(pick<4, double>(x, pb), s);  // partner's sin child
-                if (!pick<4, bool>(plus, pb)) sp = negate(sp);
-                if (live[m] && lp) nx[m] = __dadd_rn(__dmul_rn(x[m], c), sp);
-                else if (live[m]) nx[m] = __dmul_rn(x[m], c);
-                else if (lp) nx[m] = sp;
-                touched[m] = live[m] || lp;
+                sl[m] = probe_from<W>(a, M[m], ps[m], PR[m], stamp, &ea[m], &v[m], &overflow);
             }
-            PairTally t;
-            t.born = t.died = t.removed = t.claimed = 0u;
-            t.flags = 0u;
+            // owner: the smallest present member; a coset with no live member has nothing to do
+            bool own = !overflow;
+            unsigned long long any = v[0];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                if (!touched[m]) continue;  // absent before and after: no term
-                const unsigned long long out = settle<W>(p, M[m], nx[m], live[m], t, s_acc[l]);
-                live[m] = out != 0ull;
-                x[m] = from_bits(out);
+            for (int m = 1; m < 4; ++m) {
+                if (m >= gs) continue;
+                any |= v[m];
+                if (sl[m] >= 0 && key_less<W>(M[m], M[0])) own = false;
             }
-            if (t.born) atomicAdd(&s_cnt[l][0], t.born);
-            if (t.died) atomicAdd(&s_cnt[l][1], t.died);
-            if (t.removed) atomicAdd(&s_cnt[l][2], t.removed);
-            flags |= t.flags;
+            if (overflow) flags |= ST_TABLE;
+            if (own && any) {
+                double x[4];
+                bool live[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    live[m] = v[m] != 0ull;
+                    x[m] = from_bits(v[m]);
+                }
+                for (unsigned l = 0; l < L; ++l) {
+                    const RotParams& p = a.ps[r0 + l];
+                    const Key<W> q = mask_key<W>(p);
+                    const int b = key_eq<W>(q, G[1]) ? 1 : (key_eq<W>(q, G[2]) ? 2 : 3);
+                    const double c = p.c, s = p.s;
+                    bool anti[4], plus[4];
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) coset_sign<W>(p, M[m], anti[m], plus[m]);
+                    double nx[4];
+                    bool touched[4];
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        nx[m] = 0.0;
+                        touched[m] = false;
+                        if (m >= gs) continue;
+                        if (!anti[m]) {
+                            nx[m] = x[m];
+                            touched[m] = live[m];
+                            continue;
+                        }
+                        const int pb = m ^ b;
+                        const bool lp = pick<4, bool>(live, pb);
+                        double sp = __dmul_rn(pick<4, double>(x, pb), s);  // partner's sin child
+                        if (!pick<4, bool>(plus, pb)) sp = negate(sp);
+                        if (live[m] && lp) nx[m] = __dadd_rn(__dmul_rn(x[m], c), sp);
+                        else if (live[m]) nx[m] = __dmul_rn(x[m], c);
+                        else if (lp) nx[m] = sp;
+                        touched[m] = live[m] || lp;
+                    }
+                    PairTally t = empty_tally();
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        if (!touched[m]) continue;  // absent before and after: no term
+                        const unsigned long long out = settle<W>(p, M[m], nx[m], live[m], t);
+                        live[m] = out != 0ull;
+                        x[m] = from_bits(out);
+                    }
+                    if (t.removed) {
+                        shared_add_u128(s_acc[l], t.l1);
+                        shared_add_u128(s_acc[l] + 2, t.sq);
+                    }
+                    if (t.born) atomicAdd(&s_cnt[l][0], t.born);
+                    if (t.died) atomicAdd(&s_cnt[l][1], t.died);
+                    if (t.removed) atomicAdd(&s_cnt[l][2], t.removed);
+                    flags |= t.flags;
+                }
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    if (m >= gs) continue;
+                    const unsigned long long bits = live[m] ? dbits(x[m]) : 0ull;
+                    if (sl[m] >= 0) {
+                        if (bits != v[m]) store_val<W>(a.rec, (unsigned long long)sl[m], bits);
+                    } else if (bits) {
+                        bool ovf = false;
+                        const long long ns = hash_insert<W>(a, M[m], bits, ea[m], stamp, &ovf);
+                        if (ns >= 0) {
+                            ins[m] = true;
+                            ins_slot[m] = (unsigned long long)ns;
+                            ins_key[m] = M[m];
+                        } else {
+                            flags |= ST_TABLE;
+                        }
+                    }
+                }
+            }
         }
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            if (m >= gs) continue;
-            const unsigned long long bits = live[m] ? dbits(x[m]) : 0ull;
-            if (sl[m] >= 0) {
-                vout[sl[m]] = bits;
-            } else if (bits) {
-                bool ovf = false;
-                const long long ns = hash_insert<W>(a, M[m], ea[m], stamp, &ovf);
-                if (ns >= 0) {
-                    vout[ns] = bits;
-                    ++claimed;
-                } else {
-                    flags |= ST_TABLE;
-                }
+        for (int m = 1; m < 4; ++m) {
+            const unsigned long long at = list_reserve(a, ins[m]);
+            if (ins[m]) {
+                if (at < S) store_entry<W>(a.occ, at, ins_key[m], ins_slot[m], stamp);
+                else flags |= ST_TABLE;
             }
         }
     }
     if (flags) atomicOr(&s_flags, flags);
-    if (claimed) atomicAdd(&s_claimed, claimed);
     __syncthreads();
     if (threadIdx.x == 0) {
         for (unsigned l = 0; l < L; ++l) {
             HashStat* hs = a.stats + (size_t)(r0 + l) * kStatSlots + (blockIdx.x % kStatSlots);
-            atomic_add_u128(&hs->l1_lo, &hs->l1_hi, U128{s_acc[l][0], s_acc[l][1]});
-            atomic_add_u128(&hs->sq_lo, &hs->sq_hi, U128{s_acc[l][2], s_acc[l][3]});
+            red_add_limbs(hs->l1, U128{s_acc[l][0], s_acc[l][1]});
+            red_add_limbs(hs->sq, U128{s_acc[l][2], s_acc[l][3]});
             if (s_cnt[l][0]) atomicAdd(&hs->born, (unsigned long long)s_cnt[l][0]);
             if (s_cnt[l][1]) atomicAdd(&hs->died, (unsigned long long)s_cnt[l][1]);
             if (s_cnt[l][2]) atomicAdd(&hs->removed, (unsigned long long)s_cnt[l][2]);
             if (s_flags) atomicOr(&hs->flags, s_flags);
         }
-        if (s_claimed) atomicAdd(a.claimed, (unsigned long long)s_claimed);
     }
 }
 
@@ -633,8 +936,8 @@ struct HashRot {
 __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
     const unsigned r = blockIdx.x * 8u + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
     if (r >= a.rotations) return;
-    const HashStat x = a.stats[(size_t)r * kStatSlots + lane];
-    U128 l1{x.l1_lo, x.l1_hi}, sq{x.sq_lo, x.sq_hi};
+    const HashStat& x = a.stats[(size_t)r * kStatSlots + lane];
+    U128 l1 = limbs_total(x.l1), sq = limbs_total(x.sq);
     unsigned long long born = x.born, died = x.died, removed = x.removed;
     unsigned flags = x.flags;
 #pragma unroll
@@ -737,7 +1040,7 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
     // the live count can never exceed the slots claimed (a violated
     // invariant stops the step before the sort reads anything)
     if (!status && n > __ldcg(a.claimed)) status = ST_ORDER;
-    if (!status && n > a.out_cap) status = ST_CAPACITY;
+    if (!status && n > st->out_cap) status = ST_CAPACITY;
     st->status = status;
     st->n_out = 0;  // extraction counter
     if (!status) {
@@ -749,24 +1052,26 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
 }
 
 // --------------------------------------------------------------- extraction
-// Live slots of the final value buffer, in slot order per warp, appended
-// with one atomic per warp (their order is irrelevant: a sort follows).
+// Live records of the occupied-slot list, appended with one atomic per warp
+// (their order is irrelevant: a sort follows).
 template <int W>
 __global__ void __launch_bounds__(kHashBlock) k_hash_extract(HashArgs a) {
     if (__ldcg(&a.st->status)) return;
-    const unsigned long long* vf = a.vals[a.passes & 1u];
-    const unsigned long long S = a.slots;
+    const unsigned long long len = min(__ldcg(a.claimed), a.slots);
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     // every lane runs the same trip count so the warp ballots stay converged
     const unsigned long long first = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
-    for (unsigned long long base = first; base < S; base += stride) {
-        const unsigned long long slot = base + lane;
+    for (unsigned long long base = first; base < len; base += stride) {
+        const unsigned long long i = base + lane;
         bool live = false;
-        unsigned long long vb = 0;
-        if (slot < S && __ldcg(a.tags + slot) != 0u) {
-            vb = __ldcg(vf + slot);
-            live = vb != 0ull;
+        Rec<W> R;
+        if (i < len) {
+            const Entry<W> E = load_entry<W>(a.occ, i);
+            if (E.slot != kNoSlot) {
+                R = load_rec<W>(a.rec, E.slot);
+                live = R.val != 0ull;
+            }
         }
         const unsigned m = __ballot_sync(0xffffffffu, live);
         if (!m) continue;
@@ -775,8 +1080,8 @@ __global__ void __launch_bounds__(kHashBlock) k_hash_extract(HashArgs a) {
         at = __shfl_sync(0xffffffffu, at, 0);
         if (live) {
             const unsigned long long pos = at + __popc(m & lanemask_lt());
-            store_key<W>(a.ek, pos, load_key<W>(a.keys, slot));
-            a.ev[pos] = vb;
+            store_key<W>(a.ek, pos, R.key);
+            a.ev[pos] = R.val;
         }
     }
 }
@@ -848,6 +1153,10 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint64_t* sk
     __shared__ unsigned base[256];
     __shared__ unsigned wcnt[kSortBlock / 32][256];
     if (__ldcg(&a.st->status)) return;
+    if (!dk) {  // the last digit writes the step's output map
+        dk = a.st->out_keys;
+        dv = reinterpret_cast<unsigned long long*>(a.st->out_vals);
+    }
     const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
     const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -1010,9 +1319,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
         unsigned long long* vout = sv[(r + 1u) & 1u];
         const Key<W> Q = mask_key<W>(p);
         const double c = p.c, s = p.s;
-        PairTally t;
-        t.born = t.died = t.removed = t.claimed = 0;
-        t.flags = 0;
+        PairTally t = empty_tally();
         // one pass over the occupied slots present when the rotation starts
         // (keys it inserts are appended behind them)
         const int top = p.mbit[0];
@@ -1026,7 +1333,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
             bool anti, plus_k, plus_p;
             pair_signs(p, word_at<W>(K, p.i_word), word_at<W>(K, p.j_word), anti, plus_k, plus_p);
             if (!anti) {
-                vout[slot] = vb ? settle<W>(p, K, from_bits(vb), true, t, s_acc) : 0ull;
+                vout[slot] = vb ? settle<W>(p, K, from_bits(vb), true, t) : 0ull;
                 continue;
             }
             const Key<W> P = key_xor<W>(K, Q);
@@ -1055,8 +1362,8 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
                 nk = __dadd_rn(nk, sp);
                 np = __dadd_rn(__dmul_rn(vp, c), sk);
             }
-            vout[slot] = settle<W>(p, K, nk, true, t, s_acc);
-            const unsigned long long pbits = settle<W>(p, P, np, p_live, t, s_acc);
+            vout[slot] = settle<W>(p, K, nk, true, t);
+            const unsigned long long pbits = settle<W>(p, P, np, p_live, t);
             if (ps >= 0) {
                 vout[ps] = pbits;
             } else if (pbits) {
@@ -1069,14 +1376,12 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
                 }
             }
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            t.born += __shfl_down_sync(0xffffffffu, t.born, off);
-            t.died += __shfl_down_sync(0xffffffffu, t.died, off);
-            t.removed += __shfl_down_sync(0xffffffffu, t.removed, off);
-            t.flags |= __shfl_down_sync(0xffffffffu, t.flags, off);
-        }
+        warp_tally(t);
         if (lane == 0) {
+            if (t.removed) {
+                shared_add_u128(s_acc, t.l1);
+                shared_add_u128(s_acc + 2, t.sq);
+            }
             if (t.born) atomicAdd(&s_born, t.born);
             if (t.died) atomicAdd(&s_died, t.died);
             if (t.removed) atomicAdd(&s_removed, t.removed);

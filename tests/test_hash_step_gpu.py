@@ -121,22 +121,58 @@ def test_persistent_hash_step(golden_trajectories):
     assert np.array_equal(bits(ledger_vec(ra[4])), bits(ledger_vec(rb[4])))
 
 
-def test_fused_runs_match():
-    """TPGP_GB_HASH_FUSE=1: one pass per run of rotations on a site pair
-    (each coset evolved through the run) instead of one pass per rotation;
-    same maps, FIDs and ledgers."""
-    rng = np.random.default_rng(42)
-    keys, vals = random_map(rng, 40, 3000)
-    terms = H.ring_j1j2(40, 1.0, 0.3)
-    opts = options(1e-4, exact_ledger=False)
-    plain = evolve(True, 40, keys, vals, terms, 0.03, 2, opts)
+def _fused(*args):
     os.environ["TPGP_GB_HASH_FUSE"] = "1"
     try:
-        fused = evolve(True, 40, keys, vals, terms, 0.03, 2, opts)
+        return evolve(True, *args)
     finally:
         os.environ.pop("TPGP_GB_HASH_FUSE", None)
-    assert fused[0] == plain[0] == 0
-    assert np.array_equal(fused[1], plain[1])
-    assert np.array_equal(bits(fused[2]), bits(plain[2]))
-    assert np.array_equal(bits(fused[3]), bits(plain[3]))
-    assert np.array_equal(bits(ledger_vec(fused[4])), bits(ledger_vec(plain[4])))
+
+
+def _same(a, b):
+    assert a[0] == b[0] == 0, (a[5], b[5])
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(bits(a[2]), bits(b[2]))
+    assert np.array_equal(bits(a[3]), bits(b[3]))
+    assert np.array_equal(bits(ledger_vec(a[4])), bits(ledger_vec(b[4])))
+
+
+@pytest.mark.parametrize("n_spins", [16, 40, 64, 100, 120])
+def test_fused_runs_match(n_spins):
+    """TPGP_GB_HASH_FUSE=1: one pass per run of rotations on a site pair
+    (each coset evolved through the run) instead of one pass per rotation;
+    same maps, FIDs and ledgers as the sorted path, for one- to four-word
+    keys.  A Strang step's middle run is six rotations on one edge (the
+    longest run the pass takes)."""
+    rng = np.random.default_rng(42 + n_spins)
+    keys, vals = random_map(rng, n_spins, 3000)
+    terms = H.ring_j1j2(n_spins, 1.0, 0.3)
+    opts = options(1e-4, exact_ledger=False)
+    _same(_fused(n_spins, keys, vals, terms, 0.03, 2, opts),
+          evolve(False, n_spins, keys, vals, terms, 0.03, 2, opts))
+
+
+def test_fused_runs_single_generator_and_cubic():
+    """Runs whose group has one mask (an Ising-only edge list: every run is
+    ZZ on one pair, a two-member coset) and the cubic lattice's edge list."""
+    rng = np.random.default_rng(7)
+    keys, vals = random_map(rng, 24, 3000)
+    zz = [t for t in H.ring_j1j2(24, 1.0, 0.3) if t[2] == 3 and t[3] == 3]
+    opts = options(1e-4, exact_ledger=False)
+    _same(_fused(24, keys, vals, zz, 0.05, 2, opts), evolve(False, 24, keys, vals, zz, 0.05, 2, opts))
+    k0, v0 = H.single_site_operator(64, 0)
+    cubic = H.cubic_111(4)
+    copts = options(1e-5, exact_ledger=False)
+    _same(_fused(64, k0, v0, cubic, 0.005, 3, copts), evolve(False, 64, k0, v0, cubic, 0.005, 3, copts))
+
+
+def test_fused_runs_table_retry(oracle):
+    """A map that outgrows its table inside a step (8 spins, global X,
+    threshold 0): the fused passes report the full table, the step is re-run
+    on a larger one, and the result is the oracle's."""
+    terms = H.ring_j1j2(8)
+    k0, v0 = H.global_x_operator(8)
+    ost, ok, ov, _ = oracle.strang_step(k0, v0, 8, terms, 0.05, threshold=0.0, steps=3)
+    a = _fused(8, k0, v0, terms, 0.05, 3, options(0.0, exact_ledger=False))
+    assert a[0] == ost == 0, a[5]
+    assert np.array_equal(a[1], ok) and np.array_equal(bits(a[2]), bits(ov))

@@ -1,9 +1,9 @@
 """Benchmark trajectories as a command-line driver (used for profiling).
 
-    python -m ddevol_gb300.workloads --config ring16 --setup-steps 200 --steps 1 [--events]
-    python -m ddevol_gb300.workloads --config ring64 --target-terms 1e5 --save-state S.npz
-    python -m ddevol_gb300.workloads --config ring64 --load-state S.npz --steps 1
-    python -m ddevol_gb300.workloads --batch serve --items 16 --setup-steps 10 --steps 1
+    python workloads.py --config ring16 --setup-steps 200 --steps 1 [--events]
+    python workloads.py --config ring64 --target-terms 1e5 --save-state S.npz
+    python workloads.py --config ring64 --load-state tests/golden/ring64_window.npz --steps 1
+    python workloads.py --batch serve --items 16 --setup-steps 10 --steps 1
 
 Single-map mode evolves the configuration from its initial operator for
 --setup-steps Strang steps (or until the map holds --target-terms terms),
@@ -24,11 +24,15 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
+import sys
 
 import numpy as np
 
-from . import hamiltonians as H
-from .engine import Engine, GbLedger, options
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from ddevol_gb300 import hamiltonians as H  # noqa: E402
+from ddevol_gb300.engine import Engine, GbLedger, options  # noqa: E402
 
 CONFIGS = {
     "ring64": (64, lambda: H.ring_all_pairs(64), 0.005, 1e-5),
@@ -83,7 +87,7 @@ def run(config: str, setup_steps: int, steps: int, events: bool, exact_ledger: b
 
 
 def run_batch(items: int, setup_steps: int, steps: int, seed: int = 20261203):
-    from .engine import Batch
+    from ddevol_gb300.engine import Batch
     rng = np.random.default_rng(seed)
     reqs = [H.serving_request(rng) for _ in range(items)]
     eng = Engine(0)
