@@ -1,9 +1,13 @@
 """Builds the sm_103a library ``ddevol_gb300/_native/libtpgp_gb300.so`` in-tree.
 
-Two translation units compiled in parallel with nvcc, then linked:
+Translation units compiled in parallel with nvcc, then linked:
 
 * ``csrc/branch_abi.cu`` -- the reference-compatible ``tpgp_cuda_*`` ABI;
-* ``csrc/engine.cu``     -- the device-resident ``tpgp_gb_*`` ABI and kernels.
+* ``csrc/engine.cu``     -- the device-resident ``tpgp_gb_*`` ABI and kernels;
+* ``csrc/serve.cu``      -- the serving loop;
+* ``csrc/checkpoint.cu`` -- restart records in the reference's format;
+
+then the CLI front end ``cli/tpgp_gb_cli.c`` (gcc) into ``_native/tpgp_gb_cli``.
 
 Numerical flags follow the reference's contract for its CUDA backend
 (DDevol engine/cuda/CMakeLists.txt:26-27): no FMA contraction, IEEE division
@@ -22,7 +26,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_native")
 LIB = os.path.join(OUT_DIR, "libtpgp_gb300.so")
-UNITS = ["branch_abi.cu", "engine.cu", "serve.cu"]
+UNITS = ["branch_abi.cu", "engine.cu", "serve.cu", "checkpoint.cu"]
+CLI_SRC = os.path.join(HERE, "cli", "tpgp_gb_cli.c")
+CLI = os.path.join(OUT_DIR, "tpgp_gb_cli")
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
@@ -60,8 +66,10 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles the library if any source is newer than it; returns its path."""
+    """Compiles the library (and the CLI) if any source is newer; returns the library."""
     if not force and not _stale():
+        if not os.path.exists(CLI) or os.path.getmtime(CLI) < os.path.getmtime(CLI_SRC):
+            build_cli()
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     compiler = nvcc()
@@ -87,7 +95,21 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """The CLI front end (C, links the library only through include/)."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler for the CLI")
+    cmd = [cc, "-O2", "-std=c11", "-Wall", "-Wextra", "-fno-fast-math", "-ffp-contract=off",
+           "-o", CLI, CLI_SRC, "-L" + OUT_DIR, "-ltpgp_gb300", "-Wl,-rpath,$ORIGIN", "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

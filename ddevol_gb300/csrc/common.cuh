@@ -30,6 +30,14 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// ------------------------------------------------------------------ lanes
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
 // ---------------------------------------------------------------- status bits
 enum : unsigned {
     ST_NUMERIC = 1u,    // nonfinite branch value or merged sum -> ENUMERIC
@@ -352,7 +360,16 @@ struct DeviceState {
     uint64_t* out_keys;
     double* out_vals;
     unsigned long long out_cap;
+    // poll limit of every device-side wait of the call (0: the defaults), and
+    // extra arrivals a grid barrier waits for (nonzero only to test that a
+    // wait which can never end gives up: a participant that does not exist)
+    unsigned wait_polls, bar_extra;
 };
+
+__device__ __forceinline__ unsigned poll_limit(const DeviceState* st, unsigned dflt) {
+    const unsigned v = *reinterpret_cast<const volatile unsigned*>(&st->wait_polls);
+    return v ? v : dflt;
+}
 
 // --------------------------------------------------------- decoupled look-back
 // One 64-bit word per tile: [flag:2 | hi:31 | lo:31].  flag 1 = tile
@@ -387,7 +404,8 @@ __device__ __forceinline__ unsigned long long poll(const unsigned long long* slo
 __device__ inline unsigned long long lookback_exclusive(unsigned long long* tiles,
                                                         unsigned long long tile,
                                                         unsigned long long agg_packed,
-                                                        unsigned int* status) {
+                                                        unsigned int* status,
+                                                        unsigned limit = kLookbackPolls) {
     const unsigned lane = threadIdx.x & 31;
     if (tile == 0) {
         if (lane == 0) publish(tiles, kFlagPre | agg_packed);
@@ -405,7 +423,7 @@ __device__ inline unsigned long long lookback_exclusive(unsigned long long* tile
         if (t >= 0) {
             word = poll(tiles + t);
             while ((word >> 62) == 0) {
-                if (++polls > kLookbackPolls) {
+                if (++polls > limit) {
                     atomicOr(status, ST_TIMEOUT);
                     word = kFlagPre;  // give up: treat as an empty prefix
                     break;

@@ -43,6 +43,7 @@
 // at the first failure.  Work after a failing rotation is discarded: the
 // step's input map is never written (transactional).
 #pragma once
+#include "onesweep.cuh"
 #include "rotate_kernels.cuh"
 
 namespace tg {
@@ -50,7 +51,6 @@ namespace tg {
 constexpr int kHashBlock = 256;
 constexpr int kMaxProbe = 2048;  // linear-probe bound; hitting it reports ST_TABLE
 constexpr int kStatSlots = 32;   // stat slots per rotation (spreads the atomics)
-constexpr int kSortBlock = 256, kSortItems = 8, kSortTile = kSortBlock * kSortItems;
 constexpr uint32_t kNoSlot = 0xffffffffu;  // list entry reserved but not yet written
 
 // Per-rotation stat slot.  The removed-weight sums are 128-bit integers
@@ -128,7 +128,6 @@ struct HashArgs {
     unsigned long long* ev;
     uint64_t* tk;
     unsigned long long* tv;
-    unsigned* hist;                 // radix sort: digit counts / offsets, look-back words
     DeviceState* st;
 };
 
@@ -1086,118 +1085,6 @@ __global__ void __launch_bounds__(kHashBlock) k_hash_extract(HashArgs a) {
     }
 }
 
-// --------------------------------------------------------------- radix sort
-// Stable LSD radix sort of the extracted (key, value) pairs by key, 8-bit
-// digits from the least significant; the last pass writes the output map.
-template <int W>
-__device__ __forceinline__ unsigned digit_of(const Key<W>& k, int d) {
-    return (unsigned)((word_at<W>(k, d >> 3) >> ((d & 7) * 8)) & 0xffull);
-}
-
-template <int W>
-__global__ void __launch_bounds__(kSortBlock) k_radix_hist(const uint64_t* keys, HashArgs a,
-                                                           int d) {
-    __shared__ unsigned cnt[256];
-    if (__ldcg(&a.st->status)) return;
-    const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
-    if (d == 0 && blockIdx.x == 0 && threadIdx.x == 0 && __ldcg(&a.st->n_out) != n)
-        atomicOr(&a.st->status, ST_ORDER);  // extraction must find exactly the committed count
-    const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
-    for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        cnt[threadIdx.x] = 0;
-        __syncthreads();
-#pragma unroll
-        for (int e = 0; e < kSortItems; ++e) {
-            const unsigned long long i = tile * kSortTile + (unsigned long long)e * kSortBlock + threadIdx.x;
-            if (i < n) atomicAdd(&cnt[digit_of<W>(load_key<W>(keys, i), d)], 1u);
-        }
-        __syncthreads();
-        a.hist[(size_t)threadIdx.x * ntiles + tile] = cnt[threadIdx.x];
-        __syncthreads();
-    }
-}
-
-// Exclusive scan of the digit-major histogram (one CTA of 1024 threads).
-__global__ void __launch_bounds__(1024) k_radix_scan(HashArgs a) {
-    __shared__ unsigned long long s_part[1024];
-    if (__ldcg(&a.st->status)) return;
-    const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
-    const unsigned long long total = 256ull * ((n + kSortTile - 1) / kSortTile);
-    const unsigned long long per = (total + blockDim.x - 1) / blockDim.x;
-    const unsigned long long lo = min(total, per * threadIdx.x), hi = min(total, lo + per);
-    unsigned long long sum = 0;
-    for (unsigned long long i = lo; i < hi; ++i) sum += a.hist[i];
-    s_part[threadIdx.x] = sum;
-    __syncthreads();
-    for (unsigned off = 1; off < blockDim.x; off <<= 1) {
-        const unsigned long long v = threadIdx.x >= off ? s_part[threadIdx.x - off] : 0ull;
-        __syncthreads();
-        s_part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    unsigned long long run = s_part[threadIdx.x] - sum;
-    for (unsigned long long i = lo; i < hi; ++i) {
-        const unsigned c = a.hist[i];
-        a.hist[i] = (unsigned)run;
-        run += c;
-    }
-}
-
-// Stable scatter: within a tile, elements are ranked in tile order (rounds
-// of 256 consecutive elements; within a round by warp, then by lane).
-template <int W>
-__global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint64_t* sk,
-                                                              const unsigned long long* sv,
-                                                              uint64_t* dk, unsigned long long* dv,
-                                                              HashArgs a, int d) {
-    __shared__ unsigned base[256];
-    __shared__ unsigned wcnt[kSortBlock / 32][256];
-    if (__ldcg(&a.st->status)) return;
-    if (!dk) {  // the last digit writes the step's output map
-        dk = a.st->out_keys;
-        dv = reinterpret_cast<unsigned long long*>(a.st->out_vals);
-    }
-    const unsigned long long n = min(__ldcg(&a.st->n), a.slots);  // never beyond the buffers
-    const unsigned long long ntiles = (n + kSortTile - 1) / kSortTile;
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        base[threadIdx.x] = a.hist[(size_t)threadIdx.x * ntiles + tile];
-        for (int e = 0; e < kSortItems; ++e) {
-            // (the barrier at the end of the previous round separates these
-            // writes from that round's reads)
-            for (int q = lane; q < 256; q += 32) wcnt[warp][q] = 0;
-            __syncthreads();
-            const unsigned long long i = tile * kSortTile + (unsigned long long)e * kSortBlock + threadIdx.x;
-            const bool valid = i < n;
-            Key<W> k;
-            unsigned long long v = 0;
-            unsigned dig = 256;
-            if (valid) {
-                k = load_key<W>(sk, i);
-                v = __ldcg(sv + i);
-                dig = digit_of<W>(k, d);
-            }
-            const unsigned peers = __match_any_sync(0xffffffffu, dig);
-            if (valid && lane == (unsigned)(__ffs(peers) - 1)) wcnt[warp][dig] = __popc(peers);
-            __syncthreads();
-            if (valid) {
-                unsigned before = 0;
-                for (unsigned w = 0; w < warp; ++w) before += wcnt[w][dig];
-                const unsigned long long pos =
-                    (unsigned long long)base[dig] + before + __popc(peers & lanemask_lt());
-                store_key<W>(dk, pos, k);
-                dv[pos] = v;
-            }
-            __syncthreads();
-            unsigned tot = 0;
-#pragma unroll
-            for (int w = 0; w < kSortBlock / 32; ++w) tot += wcnt[w][threadIdx.x];
-            base[threadIdx.x] += tot;
-            __syncthreads();
-        }
-    }
-}
-
 // --------------------------------------------------- CTA-local batched step
 // A batched item whose whole step fits in shared memory runs it in one CTA:
 // the same pair updates as k_hash_rotate on a shared-memory table, one
@@ -1478,7 +1365,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
         s_hist[tid] = 0u;
         __syncthreads();
         for (unsigned long long i = tid; i < n; i += blockDim.x)
-            atomicAdd(&s_hist[digit_of<W>(load_key<W>(srck, i), d)], 1u);
+            atomicAdd(&s_hist[sort_digit<W>(load_key<W>(srck, i), d)], 1u);
         __syncthreads();
         // exclusive scan of the 256 counts (one per thread)
         const unsigned mine = s_hist[tid];
@@ -1505,7 +1392,7 @@ __global__ void __launch_bounds__(256) k_batch_hash(const BatchItem* items, cons
             if (valid) {
                 k = load_key<W>(srck, i);
                 v = __ldcg(srcv + i);
-                dig = digit_of<W>(k, d);
+                dig = sort_digit<W>(k, d);
             }
             const unsigned peers = __match_any_sync(0xffffffffu, dig);
             if (valid && lane == (unsigned)(__ffs(peers) - 1)) s_wcnt[warp][dig] = __popc(peers);

@@ -57,6 +57,7 @@ struct RotParams {
     int th[8];              // threshold bit positions
     int lev_lo[4], lev_hi[4];  // index in th of mbit[l] and mbit[l] + 1
     int exact_ledger;       // 1: removed values kept in order for a sequential ledger
+    unsigned wait_polls;    // device waits give up after this many polls (0: defaults)
     int fx_unit1, fx_unit2; // fixed-point units of the bound ledger (see fixed_terms)
     unsigned long long max_terms;
     double max_drop_l2;
@@ -97,12 +98,6 @@ constexpr int kCommitBlock = 1024;
 constexpr int kBlInf = 0x7fff;  // digit-boundary level of element 0
 static_assert(kP1Items * (kP1Block / 32) == 64, "P1 row/warp scan assumes 64 entries");
 
-__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
-__device__ __forceinline__ unsigned lanemask_lt() {
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
 
 // The CTAs that run a phase for one map: the whole grid (per-kernel path and
 // persistent kernel) or the CTAs of one thread-block cluster (batched maps).
@@ -183,7 +178,8 @@ __device__ void phase_classify(const RotParams& p, const Buffers& b, Grid g) {
             s_counts[2 * lane + 1] = excl + v0;
             const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
             const unsigned long long base =
-                lookback_exclusive(b.p1_tiles, tile, pack2(total, 0), &st->status);
+                lookback_exclusive(b.p1_tiles, tile, pack2(total, 0), &st->status,
+                                   poll_limit(st, kLookbackPolls));
             if (lane == 0) {
                 unsigned long long lo, hi;
                 unpack2(base, lo, hi);
@@ -903,7 +899,8 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
         }
         if (warp == 0) {
             const unsigned long long base =
-                lookback_exclusive(b.p3_tiles, tile, pack2(tk_tot, tn_tot), &st->status);
+                lookback_exclusive(b.p3_tiles, tile, pack2(tk_tot, tn_tot), &st->status,
+                                   poll_limit(st, kLookbackPolls));
             if (lane == 0) {
                 unsigned long long bk, bn;
                 unpack2(base, bk, bn);
@@ -1000,15 +997,16 @@ __device__ inline bool grid_barrier(DeviceState* st) {
         const unsigned g = *gen;
         __threadfence();
         const unsigned arrived = atomicAdd(&st->bar_count, 1u);
+        const unsigned limit = poll_limit(st, kBarrierPolls);
         int ok = 1;
-        if (arrived == gridDim.x - 1) {
+        if (arrived == gridDim.x - 1 + st->bar_extra) {
             atomicExch(&st->bar_count, 0u);
             __threadfence();
             atomicAdd(&st->bar_gen, 1u);
         } else {
             unsigned polls = 0;
             while (*gen == g) {
-                if (++polls > kBarrierPolls) {
+                if (++polls > limit) {
                     atomicOr(&st->status, ST_TIMEOUT);
                     ok = 0;
                     break;

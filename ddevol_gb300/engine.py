@@ -36,14 +36,16 @@ def _f64p(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-def options(threshold=0.0, max_terms=0, max_drop_l2=0.0, exact_ledger=True, use_graphs=True):
+def options(threshold=0.0, max_terms=0, max_drop_l2=0.0, exact_ledger=True, use_graphs=True,
+            wait_polls=0):
     """tpgp_gb_options.  exact_ledger=True: the reference's sequential
     removed-weight ledger, bitwise (sorted per-rotation kernels);
     exact_ledger=False: the fixed-point bound ledger, which also selects the
     hash-table step for maps up to 6e5 terms.  Keys, values and FIDs are the
-    same either way."""
+    same either way.  wait_polls: poll limit of the device-side waits (0:
+    the defaults)."""
     return GbOptions(float(threshold), int(max_terms), float(max_drop_l2), int(bool(exact_ledger)),
-                     int(bool(use_graphs)))
+                     int(bool(use_graphs)), int(wait_polls))
 
 
 def terms_array(terms):
@@ -233,6 +235,15 @@ class DeviceMap:
                                      C.byref(ledger), _f64p(fids) if record_fid else None,
                                      C.byref(done), err, len(err))
         return st, fids[:done.value], ledger, err.value.decode()
+
+    def liouvillian(self, terms, out=None):
+        """out <- -i[H, self] (tpgp_gb_liouvillian); out defaults to a new map
+        of the same spin count.  Returns (status, out map, message)."""
+        out = out if out is not None else self.engine.map(self.n_spins)
+        arr, count = terms_array(terms)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_liouvillian(out.ptr, self.ptr, arr, count, err, len(err))
+        return st, out, err.value.decode()
 
     def single_sum(self, pauli=1):
         out = C.c_double()

@@ -38,9 +38,26 @@ class GbLedger(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class GbCheckpoint(C.Structure):
+    """tpgp_gb_checkpoint (include/tpgp_gb300.h): a restart record in host memory."""
+
+    _fields_ = [("n_spins", C.c_size_t), ("len", C.c_size_t), ("keys", C.POINTER(C.c_uint64)),
+                ("values", C.POINTER(C.c_double)), ("terms", C.POINTER(GbTerm)),
+                ("term_count", C.c_size_t), ("threshold", C.c_double), ("max_terms", C.c_size_t),
+                ("threads", C.c_uint), ("backend", C.c_int), ("validated", C.c_int),
+                ("max_drop_l2", C.c_double), ("ledger", GbLedger), ("dt", C.c_double),
+                ("pf_bound", C.c_double), ("residual_bound", C.c_double),
+                ("max_fid_bound", C.c_double), ("step", C.c_size_t), ("total_steps", C.c_size_t),
+                ("residual_depth", C.c_int), ("initial_global", C.c_int), ("model", C.c_char * 32),
+                ("j2", C.c_double), ("linear_size", C.c_size_t), ("resumed_from_step", C.c_size_t),
+                ("prior_total_steps", C.c_size_t), ("prior_max_terms", C.c_size_t),
+                ("stop_reason", C.c_int), ("last_status", C.c_int)]
+
+
 class GbOptions(C.Structure):
     _fields_ = [("threshold", C.c_double), ("max_terms", C.c_size_t),
-                ("max_drop_l2", C.c_double), ("exact_ledger", C.c_int), ("use_graphs", C.c_int)]
+                ("max_drop_l2", C.c_double), ("exact_ledger", C.c_int), ("use_graphs", C.c_int),
+                ("wait_polls", C.c_uint)]
 
 
 class GbRequest(C.Structure):
@@ -117,6 +134,17 @@ def _bind(lib):
                                    P(GbLedger), f64p, P(sz), charp, sz]
     lib.tpgp_gb_single_sum.restype = C.c_int
     lib.tpgp_gb_single_sum.argtypes = [C.c_void_p, C.c_uint, f64p]
+    lib.tpgp_gb_checkpoint_write.restype = C.c_int
+    lib.tpgp_gb_checkpoint_write.argtypes = [charp, P(GbCheckpoint), charp, sz]
+    lib.tpgp_gb_checkpoint_load.restype = C.c_int
+    lib.tpgp_gb_checkpoint_load.argtypes = [charp, P(GbCheckpoint), charp, sz]
+    lib.tpgp_gb_checkpoint_free.argtypes = [P(GbCheckpoint)]
+    lib.tpgp_gb_map_l2.restype = C.c_int
+    lib.tpgp_gb_map_l2.argtypes = [C.c_void_p, f64p]
+    lib.tpgp_gb_strang_bound.restype = C.c_double
+    lib.tpgp_gb_strang_bound.argtypes = [P(GbTerm), sz, C.c_double]
+    lib.tpgp_gb_liouvillian.restype = C.c_int
+    lib.tpgp_gb_liouvillian.argtypes = [C.c_void_p, C.c_void_p, P(GbTerm), sz, charp, sz]
     lib.tpgp_gb_last_elapsed_ms.restype = C.c_double
     lib.tpgp_gb_last_elapsed_ms.argtypes = [C.c_void_p]
     lib.tpgp_gb_last_launches.restype = sz

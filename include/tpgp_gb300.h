@@ -64,13 +64,18 @@ typedef struct {
  *     steps of maps up to 6e5 terms run the hash-table step (one kernel per
  *     rotation, no sort; TPGP_GB_HASH=0 disables it).
  *   use_graphs = 1: each Strang step's kernel sequence is captured once as a
- *     CUDA graph and replayed. */
+ *     CUDA graph and replayed.
+ *   wait_polls: how many times a device-side wait (decoupled look-back,
+ *     grid barrier) polls before it gives up and the call returns EBACKEND
+ *     with the map unchanged; 0 selects the defaults (2^22 look-back polls,
+ *     2^24 barrier polls of ~32 ns, far beyond any wait of a healthy run). */
 typedef struct {
     double threshold;
     size_t max_terms;
     double max_drop_l2;
     int exact_ledger;
     int use_graphs;
+    unsigned wait_polls;
 } tpgp_gb_options;
 
 typedef struct tpgp_gb_context tpgp_gb_context;
@@ -132,6 +137,77 @@ tpgp_gb_status tpgp_gb_evolve(tpgp_gb_map *map, const tpgp_gb_term *terms, size_
                               double dt, size_t steps, const tpgp_gb_options *options,
                               tpgp_gb_ledger *ledger, double *fid_sums, size_t *steps_done,
                               char *error, size_t error_capacity);
+
+/* A restart record in the reference's version-2 checkpoint format
+ * (engine/include/checkpoint_rev.h:6-22, engine/src/checkpoint_rev.c:283-387
+ * save, :412-586 load): little-endian fields, the terms, the map in key
+ * order, and the SHA-256 of that payload; written through a temporary file,
+ * fsync and rename, with a .manifest.json beside it.  Host arrays; a record
+ * written here loads in the reference engine and the other way round.
+ * Zero-initialise before load; release with tpgp_gb_checkpoint_free. */
+typedef struct {
+    size_t n_spins, len;
+    uint64_t *keys;  /* keys[k * ceil(n_spins / 32) + w] */
+    double *values;
+    tpgp_gb_term *terms;
+    size_t term_count;
+    double threshold;      /* options: threshold, max_terms, threads, backend, */
+    size_t max_terms;      /* validated, max_drop_l2 (tpgp_options fields)     */
+    unsigned threads;
+    int backend, validated;
+    double max_drop_l2;
+    tpgp_gb_ledger ledger;
+    double dt, pf_bound, residual_bound, max_fid_bound;
+    size_t step, total_steps;
+    int residual_depth; /* -1: none (residual_bound is then NaN) */
+    int initial_global;
+    char model[32];
+    double j2;
+    size_t linear_size, resumed_from_step, prior_total_steps, prior_max_terms;
+    int stop_reason; /* 0 running, 1 complete, 2 walltime, 3 signal, 4 resource, 5 numerical, 6 accuracy */
+    tpgp_gb_status last_status;
+} tpgp_gb_checkpoint;
+
+/* Writes a host record (validated as the reference validates one). */
+tpgp_gb_status tpgp_gb_checkpoint_write(const char *path, const tpgp_gb_checkpoint *record,
+                                        char *error, size_t error_capacity);
+/* Reads and validates a record (checksum first); *record is replaced only on
+ * success. */
+tpgp_gb_status tpgp_gb_checkpoint_load(const char *path, tpgp_gb_checkpoint *record, char *error,
+                                       size_t error_capacity);
+void tpgp_gb_checkpoint_free(tpgp_gb_checkpoint *record);
+/* Downloads a device map and writes it with its run state as the reference
+ * CLI's save_current does (engine/src/cli_rev.c:72-106): backend 4 (CUDA),
+ * one thread, no validated mode, no residual bound. */
+tpgp_gb_status tpgp_gb_checkpoint_save(const char *path, const tpgp_gb_map *map,
+                                       const tpgp_gb_term *terms, size_t count, const char *model,
+                                       double j2, double dt, const tpgp_gb_options *options,
+                                       const tpgp_gb_ledger *ledger, double pf_bound, size_t step,
+                                       size_t total_steps, int initial_global, int stop_reason,
+                                       char *error, size_t error_capacity);
+
+/* Hilbert-Schmidt norm of the map's coefficients, sqrt(sum v^2): a
+ * deterministic device reduction in binary64 (pairs of doubles carry the
+ * sum's rounding error), within a few ulps of tpgp_map_l2's long-double sum
+ * (engine/include/tpgp_rev.h:75, engine/src/tpgp_rev.c:266-271). */
+tpgp_gb_status tpgp_gb_map_l2(const tpgp_gb_map *map, double *l2);
+
+/* Conservative third-order Strang bound per step for the ordered terms,
+ * bitwise equal to tpgp_strang_bound (engine/include/tpgp_rev.h:91-94,
+ * engine/src/tpgp_rev.c:887-961); NaN for an invalid term list.  Host
+ * arithmetic only. */
+double tpgp_gb_strang_bound(const tpgp_gb_term *terms, size_t count, double dt);
+
+/* The exact algebraic generator: *out = -i[H, in] with H = sum of the terms,
+ * in binary64 with no pruning, bitwise equal to tpgp_liouvillian
+ * (engine/include/tpgp_rev.h:88-90, engine/src/tpgp_rev.c:810-857).  Both
+ * maps live on the device, belong to one context and have the same spin
+ * count; out may be in.  EINVAL for an invalid term (when no earlier term
+ * produced a nonfinite contribution or sum, which is ENUMERIC).  out is
+ * unchanged on failure; in is never changed unless it is out. */
+tpgp_gb_status tpgp_gb_liouvillian(tpgp_gb_map *out, const tpgp_gb_map *in,
+                                   const tpgp_gb_term *terms, size_t count, char *error,
+                                   size_t error_capacity);
 
 /* Compensated sum of the coefficients whose key has Pauli weight one with
  * symbol `pauli` (1..3), bitwise equal to tpgp_map_single_sum

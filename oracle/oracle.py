@@ -145,6 +145,9 @@ class Oracle:
             C.c_double, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_double),
             C.POINTER(C.c_double)]
         lib.orc_max_threads.restype = C.c_int
+        for name in ("orc_liouvillian", "orc_liouvillian_sorted"):
+            getattr(lib, name).argtypes = [C.POINTER(MapStruct), C.POINTER(MapStruct),
+                                           C.POINTER(TermStruct), C.c_size_t]
         for name in ("orc_strang_bound", "orc_strang_bound_taylor"):
             getattr(lib, name).argtypes = [C.POINTER(TermStruct), C.c_size_t, C.c_double]
             getattr(lib, name).restype = C.c_double
@@ -236,6 +239,19 @@ class Oracle:
         self.lib.orc_map_free(C.byref(m))
         return st, n_out, secs
 
+    def liouvillian(self, keys, values, n_spins, terms, sorted_sums=False):
+        """-i[H, A] (tpgp_liouvillian, tpgp_rev.c:810-857): (status, keys, values).
+        sorted_sums: the sort-then-sum restatement (for large maps) instead of
+        sorted insertion."""
+        arr, count = terms_array(terms)
+        src = self._map(keys, values, n_spins)
+        out = self._map(np.zeros(0, np.uint64), np.zeros(0), n_spins)
+        f = self.lib.orc_liouvillian_sorted if sorted_sums else self.lib.orc_liouvillian
+        st = f(C.byref(out), C.byref(src), arr, count)
+        self.lib.orc_map_free(C.byref(src))
+        k, v = self._unmap(out)
+        return st, k, v
+
     def strang_bound(self, terms, dt, taylor_only=False):
         """Upward-rounded Strang splitting bound per step (tpgp_rev.c:875-961)."""
         arr, count = terms_array(terms)
@@ -266,7 +282,21 @@ class Reference:
         for name in ("tpgp_strang_bound", "tpgp_strang_bound_taylor"):
             getattr(lib, name).argtypes = [C.POINTER(TermStruct), C.c_size_t, C.c_double]
             getattr(lib, name).restype = C.c_double
+        lib.tpgp_liouvillian.argtypes = [C.POINTER(MapStruct), C.POINTER(MapStruct),
+                                         C.POINTER(TermStruct), C.c_size_t]
         self.lib = lib
+
+    def liouvillian(self, keys, values, n_spins, terms):
+        """The reference's own tpgp_liouvillian: (status, keys, values)."""
+        arr, count = terms_array(terms)
+        src = self._map(keys, values, n_spins)
+        out = MapStruct()
+        if self.lib.tpgp_map_init(C.byref(out), n_spins):
+            raise ValueError("tpgp_map_init failed")
+        st = self.lib.tpgp_liouvillian(C.byref(out), C.byref(src), arr, count)
+        self.lib.tpgp_map_free(C.byref(src))
+        k, v = self._unmap(out)
+        return st, k, v
 
     def strang_bound(self, terms, dt, taylor_only=False):
         arr, count = terms_array(terms)

@@ -395,6 +395,246 @@ int orc_strang_step(orc_map *map, const orc_term *terms, size_t count, double dt
     return ORC_OK;
 }
 
+/* Adds v into a sorted map the way tpgp_map_add does (tpgp_rev.c:206-243):
+ * zero v is ignored; an existing key takes RN(old + v) and disappears when
+ * that is zero; a nonfinite sum is ENUMERIC; a new key is inserted in order. */
+static int map_add_sorted(orc_map *m, const uint64_t *key, double v) {
+    if (!isfinite(v))
+        return ORC_EINVAL;
+    if (v == 0)
+        return ORC_OK;
+    const size_t w = m->n_words;
+    size_t lo = 0, hi = m->len;
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if (key_order(m->keys + mid * w, key, w) < 0)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    if (lo < m->len && key_order(m->keys + lo * w, key, w) == 0) {
+        double sum = m->values[lo] + v;
+        if (!isfinite(sum))
+            return ORC_ENUMERIC;
+        if (sum == 0) {
+            memmove(m->keys + lo * w, m->keys + (lo + 1) * w, (m->len - lo - 1) * w * sizeof(uint64_t));
+            memmove(m->values + lo, m->values + lo + 1, (m->len - lo - 1) * sizeof(double));
+            m->len--;
+        } else {
+            m->values[lo] = sum;
+        }
+        return ORC_OK;
+    }
+    if (m->len == m->capacity) {
+        size_t cap = m->capacity ? 2 * m->capacity : 16;
+        uint64_t *k = realloc(m->keys, cap * w * sizeof(uint64_t));
+        if (!k)
+            return ORC_ENOMEM;
+        m->keys = k;
+        double *vals = realloc(m->values, cap * sizeof(double));
+        if (!vals)
+            return ORC_ENOMEM;
+        m->values = vals;
+        m->capacity = cap;
+    }
+    memmove(m->keys + (lo + 1) * w, m->keys + lo * w, (m->len - lo) * w * sizeof(uint64_t));
+    memmove(m->values + lo + 1, m->values + lo, (m->len - lo) * sizeof(double));
+    memcpy(m->keys + lo * w, key, w * sizeof(uint64_t));
+    m->values[lo] = v;
+    m->len++;
+    return ORC_OK;
+}
+
+/* The exact algebraic generator -i[H, A] in binary64, no pruning
+ * (tpgp_liouvillian, tpgp_rev.c:810-857): for each term in array order (an
+ * invalid term is EINVAL when reached), for each input key in key order, an
+ * anticommuting key contributes (2h) * v * (+1 if the phase exponent is 1,
+ * else -1) to key xor (qi@i, qj@j), added in that order; a nonfinite
+ * contribution or sum is ENUMERIC.  `out` is replaced only on success. */
+int orc_liouvillian(orc_map *out, const orc_map *in, const orc_term *terms, size_t count) {
+    if (!out || !in || (!terms && count))
+        return ORC_EINVAL;
+    orc_map tmp;
+    memset(&tmp, 0, sizeof(tmp));
+    tmp.n_spins = in->n_spins;
+    tmp.n_words = in->n_words;
+    const size_t w = in->n_words;
+    uint64_t *key = malloc(w * sizeof(uint64_t));
+    if (!key)
+        return ORC_ENOMEM;
+    int status = ORC_OK;
+    for (size_t t = 0; t < count && !status; t++) {
+        const orc_term *q = terms + t;
+        if (q->i >= in->n_spins || q->j >= in->n_spins || q->i == q->j || q->qi > 3 || q->qj > 3 ||
+            !isfinite(q->h)) {
+            status = ORC_EINVAL;
+            break;
+        }
+        for (size_t k = 0; k < in->len; k++) {
+            const uint64_t *p = in->keys + k * w;
+            unsigned pi = site_symbol(p, q->i), pj = site_symbol(p, q->j);
+            if (!(anticommutes(q->qi, pi) ^ anticommutes(q->qj, pj)))
+                continue;
+            unsigned phase = (phase_of(q->qi, pi) + phase_of(q->qj, pj)) & 3u;
+            double v = 2 * q->h * in->values[k] * (phase == 1 ? 1 : -1);
+            if (!isfinite(v)) {
+                status = ORC_ENUMERIC;
+                break;
+            }
+            memcpy(key, p, w * sizeof(uint64_t));
+            key[q->i / 32] ^= (uint64_t)q->qi << (2 * (q->i % 32));
+            key[q->j / 32] ^= (uint64_t)q->qj << (2 * (q->j % 32));
+            status = map_add_sorted(&tmp, key, v);
+            if (status)
+                break;
+        }
+    }
+    free(key);
+    if (status) {
+        orc_map_free(&tmp);
+        return status;
+    }
+    if (!tmp.keys) { /* empty result: keep a valid allocation */
+        tmp.keys = malloc(w * sizeof(uint64_t));
+        tmp.values = malloc(sizeof(double));
+        tmp.capacity = 1;
+        if (!tmp.keys || !tmp.values) {
+            orc_map_free(&tmp);
+            return ORC_ENOMEM;
+        }
+    }
+    orc_map_free(out);
+    *out = tmp;
+    return ORC_OK;
+}
+
+/* The same generator for maps too large for sorted insertion: every
+ * contribution in the reference's addition order (term, then input key),
+ * a stable merge sort by output key, then one sequential RN sum per key in
+ * that order, kept when nonzero.  A key's running sum is the one
+ * tpgp_map_add keeps (a cancellation to zero removes the key, and the next
+ * contribution then starts from it exactly as from zero).  Contributions stop
+ * at the first invalid term or nonfinite contribution; a nonfinite sum among
+ * those generated precedes the stop, so it is ENUMERIC.  Checked against
+ * orc_liouvillian on the reference's golden cases. */
+int orc_liouvillian_sorted(orc_map *out, const orc_map *in, const orc_term *terms, size_t count) {
+    if (!out || !in || (!terms && count))
+        return ORC_EINVAL;
+    const size_t w = in->n_words;
+    int stop = ORC_OK;
+    size_t total = 0, valid = 0;
+    for (; valid < count; valid++) {
+        const orc_term *q = terms + valid;
+        if (q->i >= in->n_spins || q->j >= in->n_spins || q->i == q->j || q->qi > 3 || q->qj > 3 ||
+            !isfinite(q->h)) {
+            stop = ORC_EINVAL;
+            break;
+        }
+        for (size_t k = 0; k < in->len; k++) {
+            const uint64_t *p = in->keys + k * w;
+            if (anticommutes(q->qi, site_symbol(p, q->i)) ^ anticommutes(q->qj, site_symbol(p, q->j)))
+                total++;
+        }
+    }
+    uint64_t *ck = malloc((total ? total : 1) * w * sizeof(uint64_t));
+    double *cv = malloc((total ? total : 1) * sizeof(double));
+    size_t *idx = malloc((total ? total : 1) * sizeof(size_t));
+    size_t *tmp = malloc((total ? total : 1) * sizeof(size_t));
+    int status = ORC_OK;
+    if (!ck || !cv || !idx || !tmp) {
+        status = ORC_ENOMEM;
+        goto done;
+    }
+    size_t a = 0;
+    for (size_t t = 0; t < valid && !status; t++) {
+        const orc_term *q = terms + t;
+        for (size_t k = 0; k < in->len; k++) {
+            const uint64_t *p = in->keys + k * w;
+            unsigned pi = site_symbol(p, q->i), pj = site_symbol(p, q->j);
+            if (!(anticommutes(q->qi, pi) ^ anticommutes(q->qj, pj)))
+                continue;
+            unsigned phase = (phase_of(q->qi, pi) + phase_of(q->qj, pj)) & 3u;
+            double v = 2 * q->h * in->values[k] * (phase == 1 ? 1 : -1);
+            if (!isfinite(v)) {
+                status = ORC_ENUMERIC;
+                break;
+            }
+            memcpy(ck + a * w, p, w * sizeof(uint64_t));
+            ck[a * w + q->i / 32] ^= (uint64_t)q->qi << (2 * (q->i % 32));
+            ck[a * w + q->j / 32] ^= (uint64_t)q->qj << (2 * (q->j % 32));
+            cv[a] = v;
+            idx[a] = a;
+            a++;
+        }
+    }
+    if (status)
+        goto done;
+    {
+        size_t *x0 = idx, *y0 = tmp;
+        for (size_t width = 1; width < a; width *= 2) {
+            for (size_t lo = 0; lo < a; lo += 2 * width) {
+                size_t mid = lo + width < a ? lo + width : a;
+                size_t hi = lo + 2 * width < a ? lo + 2 * width : a;
+                size_t x = lo, y = mid, o = lo;
+                while (x < mid && y < hi) {
+                    if (key_order(ck + x0[x] * w, ck + x0[y] * w, w) <= 0)
+                        y0[o++] = x0[x++];
+                    else
+                        y0[o++] = x0[y++];
+                }
+                while (x < mid)
+                    y0[o++] = x0[x++];
+                while (y < hi)
+                    y0[o++] = x0[y++];
+            }
+            size_t *t = x0;
+            x0 = y0;
+            y0 = t;
+        }
+        if (x0 != idx)
+            memcpy(idx, x0, a * sizeof(size_t));
+    }
+    orc_map res;
+    memset(&res, 0, sizeof(res));
+    res.n_spins = in->n_spins;
+    res.n_words = w;
+    res.keys = malloc((a ? a : 1) * w * sizeof(uint64_t));
+    res.values = malloc((a ? a : 1) * sizeof(double));
+    res.capacity = a ? a : 1;
+    if (!res.keys || !res.values) {
+        orc_map_free(&res);
+        status = ORC_ENOMEM;
+        goto done;
+    }
+    for (size_t k = 0; k < a;) {
+        const size_t first = idx[k++];
+        double v = cv[first];
+        while (k < a && key_order(ck + first * w, ck + idx[k] * w, w) == 0) {
+            v += cv[idx[k++]];
+            if (!isfinite(v))
+                status = ORC_ENUMERIC;
+        }
+        if (v != 0) {
+            memcpy(res.keys + res.len * w, ck + first * w, w * sizeof(uint64_t));
+            res.values[res.len++] = v;
+        }
+    }
+    if (!status)
+        status = stop;
+    if (status) {
+        orc_map_free(&res);
+    } else {
+        orc_map_free(out);
+        *out = res;
+    }
+done:
+    free(ck);
+    free(cv);
+    free(idx);
+    free(tmp);
+    return status;
+}
+
 /* Compensated long-double sum of coefficients whose key has Pauli weight 1
  * with symbol p (tpgp_rev.c:311-338). */
 double orc_single_sum(const orc_map *m, unsigned p) {
