@@ -47,6 +47,7 @@ enum : unsigned {
     ST_TIMEOUT = 16u,   // a bounded wait gave up -> EBACKEND
     ST_ORDER = 32u,     // input keys not strictly ascending / padding bits -> EINVAL
     ST_TABLE = 64u,     // hash-table step: probe bound hit; host enlarges the table and retries
+    ST_LOG = 128u,      // exact-ledger log of removed values too small: host enlarges it and retries
 };
 
 // Maximum number of map terms a device map may hold (counts are packed
@@ -360,6 +361,9 @@ struct DeviceState {
     uint64_t* out_keys;
     double* out_vals;
     unsigned long long out_cap;
+    // exact ledger: next free position of the call's log of removed |v|, and
+    // the size a retry needs when the log ran out
+    unsigned long long log_pos, log_need;
     // poll limit of every device-side wait of the call (0: the defaults), and
     // extra arrivals a grid barrier waits for (nonzero only to test that a
     // wait which can never end gives up: a participant that does not exist)

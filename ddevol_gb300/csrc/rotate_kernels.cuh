@@ -58,6 +58,7 @@ struct RotParams {
     int lev_lo[4], lev_hi[4];  // index in th of mbit[l] and mbit[l] + 1
     int exact_ledger;       // 1: removed values kept in order for a sequential ledger
     unsigned wait_polls;    // device waits give up after this many polls (0: defaults)
+    unsigned index;         // position in the call's rotation list
     int fx_unit1, fx_unit2; // fixed-point units of the bound ledger (see fixed_terms)
     unsigned long long max_terms;
     double max_drop_l2;
@@ -86,6 +87,21 @@ struct Buffers {
     unsigned long long* p3_tiles;
     DeviceState* st;
     unsigned long long cap;        // terms each map / child buffer holds
+    // exact ledger of a single map: every rotation's removed |v| in key order
+    // is appended to `log` (the tile's place from a third look-back channel,
+    // p3r_tiles) and its place recorded in rot_log[p.index]; the sequential
+    // sums run after the call (k_exact_chains).  log == nullptr: the sums run
+    // in the committing CTA (batched items).
+    double* log;
+    unsigned long long log_cap;
+    unsigned long long* p3r_tiles;
+    struct RotLog* rot_log;
+};
+
+// One rotation's entry in the exact-ledger log.
+struct RotLog {
+    unsigned long long off, count;  // its removed |v| in log[off, off + count), key order
+    unsigned counted, pad;          // 0: a no-op rotation of an empty map (no ledger change)
 };
 
 constexpr int kP1Block = 256, kP1Items = 8, kP1Tile = kP1Block * kP1Items;
@@ -589,8 +605,21 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
     const unsigned status = c_status;
     const unsigned long long n = c_n;
     double l1 = 0.0, sq = 0.0;
+    const bool logged = p.exact_ledger && b.log;
     if (!status && n > 0) {
-        if (p.exact_ledger) {
+        if (logged) {
+            // the sums run after the call; record where this rotation's values are
+            if (threadIdx.x == 0) {
+                const unsigned long long pos = __ldcg(&st->log_pos), cnt = __ldcg(&st->removed);
+                if (pos + cnt > b.log_cap) {
+                    atomicOr(&st->status, ST_LOG);
+                    st->log_need = pos + cnt;
+                } else {
+                    b.rot_log[p.index] = RotLog{pos, cnt, 1u, 0u};
+                    st->log_pos = pos + cnt;
+                }
+            }
+        } else if (p.exact_ledger) {
             // the reference's sequential order: key order = tile order, one thread
             if (threadIdx.x == 0) {
                 for (unsigned long long t = 0; t < ntiles; ++t) {
@@ -645,18 +674,25 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
             next.removal_events = __ldcg(&st->ledger.removal_events);
             next.peak_terms = __ldcg(&st->ledger.peak_terms);
             next.arithmetic_enclosed = __ldcg(&st->ledger.arithmetic_enclosed);
+            if (!fail && __ldcg(&st->status) & ST_LOG) fail = ST_LOG;
             if (!fail) {
-                const double l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
-                next.dropped_l1 = up_add(next.dropped_l1, l1);
-                next.dropped_l2 = up_add(next.dropped_l2, l2);
-                next.dropped_l2_squared = up_add(next.dropped_l2_squared, sq);
-                next.arithmetic_l2 = up_add(next.arithmetic_l2, 0.0);
+                if (!logged) {
+                    const double l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
+                    next.dropped_l1 = up_add(next.dropped_l1, l1);
+                    next.dropped_l2 = up_add(next.dropped_l2, l2);
+                    next.dropped_l2_squared = up_add(next.dropped_l2_squared, sq);
+                    next.arithmetic_l2 = up_add(next.arithmetic_l2, 0.0);
+                }
                 next.rotations += 1;
                 if (removed) next.removal_events += 1;
                 if (n_out > next.peak_terms) next.peak_terms = n_out;
                 next.arithmetic_enclosed = 0;
-                if (!is_finite(next.dropped_l2) || !is_finite(next.arithmetic_l2)) fail = ST_NUMERIC;
-                else if (p.max_drop_l2 != 0.0 && next.dropped_l2 > p.max_drop_l2) fail = ST_BUDGET;
+                // with the log, the removed-weight sums and their checks
+                // (ENUMERIC, EBUDGET) follow in rotation order after the call
+                if (!logged) {
+                    if (!is_finite(next.dropped_l2) || !is_finite(next.arithmetic_l2)) fail = ST_NUMERIC;
+                    else if (p.max_drop_l2 != 0.0 && next.dropped_l2 > p.max_drop_l2) fail = ST_BUDGET;
+                }
             }
             if (fail) {
                 atomicOr(&st->status, fail);
@@ -671,6 +707,7 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
     } else if (!status && threadIdx.x == 0) {
         st->rotations_done = __ldcg(&st->rotations_done) + 1;  // empty map: no-op, no ledger change
         st->a = 0;
+        if (logged) b.rot_log[p.index] = RotLog{0ull, 0ull, 0u, 0u};
     }
     __syncthreads();
     // clear the look-back words this rotation used (clamped to the arrays)
@@ -680,6 +717,8 @@ __device__ void commit_rotation(const RotParams& p, const Buffers& b, unsigned l
     const unsigned long long t3 = min(ntiles, t3_max);
     for (unsigned long long t = threadIdx.x; t <= t1; t += NT) b.p1_tiles[t] = 0;
     for (unsigned long long t = threadIdx.x; t <= t3; t += NT) b.p3_tiles[t] = 0;
+    if (logged)
+        for (unsigned long long t = threadIdx.x; t <= t3; t += NT) b.p3r_tiles[t] = 0;
     if (threadIdx.x == 0) {
         st->p1_counter = 0;
         st->p3_counter = 0;
@@ -705,7 +744,7 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
     uint64_t* s_fk = s_kk + (size_t)T * W;                        // sorted flipped keys
     double* s_kv = reinterpret_cast<double*>(s_fk + (size_t)T * W);
     double* s_fv = s_kv + T;
-    __shared__ unsigned long long s_tile, s_base_k, s_base_n;
+    __shared__ unsigned long long s_tile, s_base_k, s_base_n, s_base_r;
     __shared__ unsigned s_wk[NW], s_wn[NW], s_wr[NW];
     __shared__ U128 s_l1[NW], s_sq[NW];
     __shared__ int s_last;
@@ -919,12 +958,24 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
                 }
                 b.rem_count[tile] = tr_tot;
                 if (tr_tot) atomicAdd(&st->removed, (unsigned long long)tr_tot);
+                s_base_r = 0;
                 if (tile == ntiles - 1) {
                     const unsigned long long n_out = bk + tk_tot, a_next = bn + tn_tot;
                     st->n_out = n_out;
                     st->a_next = a_next;
                     if (p.has_next && n_out + a_next > b.cap) atomicOr(&st->status, ST_CAPACITY);
                 }
+            }
+        }
+        if (p.exact_ledger && b.log && warp == 0) {
+            // this tile's place among the rotation's removed values (key order)
+            const unsigned long long rb = lookback_exclusive(b.p3r_tiles, tile, pack2(tr_tot, 0),
+                                                             &st->status, poll_limit(st, kLookbackPolls));
+            if (lane == 0) {
+                unsigned long long r0, r1;
+                unpack2(rb, r0, r1);
+                s_base_r = __ldcg(&st->log_pos) + r0;
+                if (s_base_r + tr_tot > b.log_cap) atomicOr(&st->status, ST_LOG);
             }
         }
         __syncthreads();
@@ -956,7 +1007,13 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
                     ++on;
                 }
             } else {
-                if (p.exact_ledger) b.rem[tile * (unsigned long long)T + orr] = abs_of(val[e]);
+                if (p.exact_ledger) {
+                    if (!b.log) {
+                        b.rem[tile * (unsigned long long)T + orr] = abs_of(val[e]);
+                    } else if (s_base_r + orr < b.log_cap) {
+                        b.log[s_base_r + orr] = abs_of(val[e]);
+                    }
+                }
                 ++orr;
             }
         }
@@ -971,6 +1028,75 @@ __device__ void phase_merge(const RotParams& p, const Buffers& b, unsigned char*
     if (!s_last) return;
     __threadfence();
     commit_rotation<kP3Block>(p, b, ntiles);
+}
+
+// ------------------------------------------------ exact ledger after the call
+// One thread per rotation: the reference's sequential removed-weight sums
+// (engine/src/tpgp_rev.c:716-729 and upper_l2, :43-63, without MPFR) over the
+// rotation's logged |v| in key order: l1 = upadd(l1, v), sq = upadd(sq,
+// upmul(v, v)).  Values are loaded eight at a time ahead of the chain.
+struct ChainSums {
+    double l1, sq;
+};
+__global__ void __launch_bounds__(128) k_exact_chains(const double* log, const RotLog* rot_log,
+                                                     const DeviceState* st, ChainSums* sums) {
+    const unsigned long long done = __ldcg(&st->rotations_done);
+    const unsigned long long r = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= done) return;
+    const RotLog e = rot_log[r];
+    double l1 = 0.0, sq = 0.0;
+    if (e.counted) {
+        unsigned long long k = 0;
+        for (; k + 8 <= e.count; k += 8) {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = __ldcg(log + e.off + k + q);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                l1 = up_add(l1, v[q]);
+                sq = up_add(sq, up_mul(v[q], v[q]));
+            }
+        }
+        for (; k < e.count; ++k) {
+            const double v = __ldcg(log + e.off + k);
+            l1 = up_add(l1, v);
+            sq = up_add(sq, up_mul(v, v));
+        }
+    }
+    sums[r] = ChainSums{l1, sq};
+}
+
+// One thread: the ledger update of commit_rotation (tpgp_rev.c:730-753) for
+// the committed rotations in order, with its ENUMERIC and EBUDGET checks.
+// The first rotation that fails decides the call's status, ahead of any
+// failure a later rotation reported while the sums were deferred; the step
+// is transactional, so the map is discarded as the reference discards it.
+__global__ void k_exact_walk(const RotLog* rot_log, const ChainSums* sums, DeviceState* st,
+                             double max_drop_l2) {
+    const unsigned long long done = st->rotations_done;
+    Ledger led = st->ledger;
+    unsigned fail = 0;
+    for (unsigned long long r = 0; r < done && !fail; ++r) {
+        if (!rot_log[r].counted) continue;  // empty map: no ledger change
+        const ChainSums x = sums[r];
+        const double l2 = x.sq == 0.0 ? 0.0 : next_up(sqrt(x.sq));
+        led.dropped_l1 = up_add(led.dropped_l1, x.l1);
+        led.dropped_l2 = up_add(led.dropped_l2, l2);
+        led.dropped_l2_squared = up_add(led.dropped_l2_squared, x.sq);
+        led.arithmetic_l2 = up_add(led.arithmetic_l2, 0.0);
+        if (!is_finite(led.dropped_l2) || !is_finite(led.arithmetic_l2)) fail = ST_NUMERIC;
+        else if (max_drop_l2 != 0.0 && led.dropped_l2 > max_drop_l2) fail = ST_BUDGET;
+    }
+    const unsigned status = st->status;
+    const unsigned infra = ST_CAPACITY | ST_LOG | ST_TIMEOUT | ST_ORDER;
+    if (fail && !(status & infra)) {
+        st->status = fail;
+    } else if (!status) {
+        st->ledger.dropped_l1 = led.dropped_l1;
+        st->ledger.dropped_l2 = led.dropped_l2;
+        st->ledger.dropped_l2_squared = led.dropped_l2_squared;
+        st->ledger.arithmetic_l2 = led.arithmetic_l2;
+    }
 }
 
 template <int W>

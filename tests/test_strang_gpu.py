@@ -206,3 +206,36 @@ def test_with_programmatic_launch(ring16_60_oracle):
         assert np.array_equal(bits(fids), bits(fids_o))
     finally:
         os.environ.pop("TPGP_GB_PDL", None)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_first_failure_in_rotation_order(engine, oracle, exact):
+    """A step whose drop budget runs out at one rotation and whose term cap
+    would be hit at a later one reports the earlier failure, as the reference
+    does (its step stops at the first failing rotation); with the cap first,
+    ECAP.  The exact ledger's sums run after the rotations, so this checks
+    that the deferred walk puts the failures back in rotation order."""
+    g_terms = H.ring_j1j2(16)
+    k0, v0 = H.single_site_operator(16)
+    st, k20, v20, led20 = oracle.strang_step(k0, v0, 16, g_terms, 0.01, threshold=1e-6, steps=20)
+    assert st == 0
+    st, k21, v21, led21 = oracle.strang_step(k20, v20, 16, g_terms, 0.01, threshold=1e-6, steps=1)
+    grown = max(len(v21), len(v20))
+    step_drop = led21.dropped_l2  # the 21st step's total removed weight (from zero)
+    cases = [
+        # budget runs out early in the step, the cap only at its largest map
+        dict(max_drop_l2=step_drop * 0.05, max_terms=grown - 1),
+        # the cap is hit almost at once, the budget only near the end
+        dict(max_drop_l2=step_drop * 0.95, max_terms=len(v20) + 1),
+    ]
+    for lim in cases:
+        ost, _, _, _ = oracle.strang_step(k20, v20, 16, g_terms, 0.01, threshold=1e-6,
+                                          max_terms=lim["max_terms"], max_drop_l2=lim["max_drop_l2"])
+        assert ost in (3, 6)
+        m = engine.map(16, k20, v20)
+        st, led, msg = m.strang_step(g_terms, 0.01, options(1e-6, exact_ledger=exact, **lim),
+                                     GbLedger())
+        k, v = m.download()
+        m.close()
+        assert st == ost, (lim, st, ost, msg)
+        assert np.array_equal(k, k20) and np.array_equal(bits(v), bits(v20))
