@@ -43,6 +43,8 @@
 // at the first failure.  Work after a failing rotation is discarded: the
 // step's input map is never written (transactional).
 #pragma once
+#include <cooperative_groups.h>
+
 #include "onesweep.cuh"
 #include "rotate_kernels.cuh"
 
@@ -129,7 +131,32 @@ struct HashArgs {
     uint64_t* tk;
     unsigned long long* tv;
     DeviceState* st;
+    // exact ledger: every removed term's (key, rotation) as W + 1 words and
+    // its |v| bits, appended in any order (xlog == nullptr: bound ledger)
+    uint64_t* xlog_keys;
+    unsigned long long* xlog_vals;
+    unsigned long long xlog_cap;
+    unsigned long long* xlog_count;
 };
+
+// Appends a removed term (the exact ledger sorts the log by rotation, then
+// key, before it sums: the reference's order).
+template <int W>
+__device__ __forceinline__ void log_removed(const HashArgs& a, unsigned r, const Key<W>& key,
+                                            double x) {
+    // one counter for the whole step: the threads that log together take
+    // their positions with one atomic
+    const cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
+    unsigned long long pos = 0;
+    if (g.thread_rank() == 0) pos = atomicAdd(a.xlog_count, (unsigned long long)g.size());
+    pos = g.shfl(pos, 0) + g.thread_rank();
+    if (pos >= a.xlog_cap) return;  // counted: the step reports the log full
+    uint64_t* k = a.xlog_keys + pos * (W + 1);
+#pragma unroll
+    for (int w = 0; w < W; ++w) k[w] = key.w[w];
+    k[W] = r;
+    a.xlog_vals[pos] = abs_bits(x);
+}
 
 // Record layout: words 0..W-1 the key, word W the value bits, the low half
 // of word W+1 the tag.
@@ -587,6 +614,8 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
                 if (v) {
                     const unsigned long long out = settle<W>(p, E.key, from_bits(v), true, t);
                     if (out != v) store_val<W>(a.rec, E.slot, out);
+                    if (a.xlog_keys && !out && !is_zero(from_bits(v)))
+                        log_removed<W>(a, r, E.key, from_bits(v));
                 }
             }
         }
@@ -653,6 +682,10 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
                     }
                     const unsigned long long kbits = settle<W>(p, K, nk, k_live, t);
                     pbits = settle<W>(p, P, np, p_live, t);
+                    if (a.xlog_keys) {
+                        if (!kbits && !is_zero(nk)) log_removed<W>(a, r, K, nk);
+                        if (!pbits && !is_zero(np)) log_removed<W>(a, r, P, np);
+                    }
                     if (kbits != R.val) store_val<W>(a.rec, slot, kbits);
                     if (found >= 0) {
                         if (pbits != pb) store_val<W>(a.rec, (unsigned long long)found, pbits);
@@ -962,6 +995,44 @@ __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
     }
 }
 
+// Exact ledger: after the log is sorted by (rotation, key), one thread per
+// rotation finds its run and adds it in key order exactly as the reference's
+// merge loop does (tpgp_rev.c:716-729, upper_l2 :43-63 without MPFR):
+// l1 = upadd(l1, |v|), sq = upadd(sq, upmul(|v|, |v|)), l2 = nextUp(sqrt(sq)).
+// A log that overflowed reports ST_LOG (the host re-runs the step with a
+// larger one).
+template <int W>
+__global__ void __launch_bounds__(128) k_hash_xchains(HashArgs a, const uint64_t* keys,
+                                                     const unsigned long long* vals, HashRot* rot) {
+    const unsigned long long total = *a.xlog_count;
+    const unsigned r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (total > a.xlog_cap) {
+        if (r == 0) atomicOr(&a.st->status, ST_LOG);
+        return;
+    }
+    if (r >= a.rotations) return;
+    // first entry of rotation r and of rotation r + 1 (the rotation is word W)
+    auto lower = [&](unsigned long long target) {
+        unsigned long long lo = 0, hi = total;
+        while (lo < hi) {
+            const unsigned long long mid = (lo + hi) / 2;
+            if (__ldcg(keys + mid * (W + 1) + W) < target) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    };
+    const unsigned long long b = lower(r), e = lower((unsigned long long)r + 1);
+    double l1 = 0.0, sq = 0.0;
+    for (unsigned long long k = b; k < e; ++k) {
+        const double v = from_bits(__ldcg(vals + k));
+        l1 = up_add(l1, v);
+        sq = up_add(sq, up_mul(v, v));
+    }
+    rot[r].l1 = l1;
+    rot[r].sq = sq;
+    rot[r].l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
+}
+
 // One CTA.  Walks the rotations in order on one thread with the commit of
 // commit_rotation: table overflow, ENUMERIC (nonfinite merged values), ECAP,
 // ledger update, ENUMERIC (ledger), EBUDGET; an empty map is a no-op rotation
@@ -995,6 +1066,10 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
                 const HashRot& h = s_rot[k];
                 if (h.flags & ST_TABLE) {
                     status = ST_TABLE;
+                    break;
+                }
+                if (__ldcg(&st->status) & ST_LOG) {  // exact-ledger log too small
+                    status = ST_LOG;
                     break;
                 }
                 if (h.flags & ST_NUMERIC) {
