@@ -256,6 +256,85 @@ __device__ __forceinline__ double up_mul(double a, double b) {
     return next_up(__dmul_rn(a, b));
 }
 
+// A chain of up_add over the lanes' addends, in lane order, computed by the
+// warp together with the same result bits as the sequential chain:
+// returns up_add(...up_add(up_add(s, x_0), x_1)..., x_31) over the lanes
+// with `has` (warp-uniform s in, warp-uniform result out) and sets *mine to
+// the chain's value after this lane's addend.  Every lane of the warp calls.
+//
+// While s stays in one binade [2^(E-1023), 2^(E-1022)) (E its biased
+// exponent, E >= 1) its values are the integers bits(s) + k on a grid of ulp
+// 2^(E-1075).  An addend x >= 0 whose exponent is at most E adds
+// round(x / ulp) grid steps when s + x stays in the binade (round to
+// nearest; an exact half is a tie whose direction depends on s's last bit),
+// and next_up adds one more.  So each lane's step count is known without the
+// chain, an inclusive warp scan of the counts gives every lane's result as
+// bits, and the scan is valid up to the first lane whose result would leave
+// the binade, whose addend is a tie, larger than s's binade, zero-exponent s,
+// or not finite: that lane's step is taken with up_add itself, and the scan
+// resumes after it with the new s.  A zero addend is no step (up_add(s, 0) = s).
+__device__ __forceinline__ double warp_up_sum(double s, double x, bool has, double* mine) {
+    constexpr unsigned long long kMant = (1ull << 52) - 1;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned start = 0;
+    double my = s;
+    for (;;) {
+        const unsigned long long sb = dbits(s);
+        const unsigned long long E = sb >> 52;  // >= 2047 for a negative or nonfinite s
+        const bool pend = has && lane >= start;
+        unsigned long long inc = 0;
+        bool flag = false;
+        if (pend && !is_zero(x)) {
+            const unsigned long long xb = dbits(x);
+            const unsigned long long Ex = xb >> 52;
+            if (E == 0 || E >= 2047 || Ex >= 2047) {
+                flag = true;
+            } else {
+                const unsigned long long Mx = (xb & kMant) | (Ex ? (1ull << 52) : 0ull);
+                const unsigned long long Exe = Ex ? Ex : 1ull;  // subnormal x: exponent 1, no implicit bit
+                if (Exe > E) {
+                    flag = true;
+                } else {
+                    const unsigned long long d = E - Exe;
+                    unsigned long long q = 0;
+                    if (d == 0) {
+                        q = Mx;
+                    } else if (d < 64) {
+                        q = Mx >> d;
+                        const unsigned long long rem = Mx & ((1ull << d) - 1), half = 1ull << (d - 1);
+                        if (rem > half) ++q;
+                        else if (rem == half) flag = true;
+                    }
+                    inc = q + 1;
+                }
+            }
+        }
+        unsigned long long S = inc;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, S, off);
+            if (lane >= (unsigned)off) S += y;
+        }
+        const unsigned long long B = (E + 1) << 52;
+        const bool bad = pend && (flag || sb + S >= B);
+        const unsigned m = __ballot_sync(0xffffffffu, bad);
+        const unsigned L = m ? (unsigned)(__ffs(m) - 1) : 32u;
+        if (lane >= start && lane < L) my = from_bits(sb + S);
+        if (!m) {
+            s = from_bits(sb + __shfl_sync(0xffffffffu, S, 31));
+            break;
+        }
+        const unsigned long long before = sb + __shfl_sync(0xffffffffu, S - inc, L);
+        const double xl = __shfl_sync(0xffffffffu, x, L);
+        s = up_add(from_bits(before), xl);
+        if (lane == L) my = s;
+        start = L + 1;
+        if (start >= 32) break;
+    }
+    if (mine) *mine = my;
+    return s;
+}
+
 // ------------------------------------------------- fixed-point ledger sums
 // Upper bounds on sums of removed |v| and v^2 in 128-bit integer fixed
 // point: each addend is rounded UP to a multiple of 2^unit, the sum is exact

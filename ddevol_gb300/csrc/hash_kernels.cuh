@@ -131,19 +131,19 @@ struct HashArgs {
     uint64_t* tk;
     unsigned long long* tv;
     DeviceState* st;
-    // exact ledger: every removed term's (key, rotation) as W + 1 words and
-    // its |v| bits, appended in any order (xlog == nullptr: bound ledger)
+    // exact ledger: every removed term's key (W words) and |v| bits.  The
+    // passes of a step run in rotation order, so each rotation's entries form
+    // one contiguous segment of the log (in any order within it), of the
+    // length its stat slots count as removed.  xlog_keys == nullptr: bound ledger.
     uint64_t* xlog_keys;
     unsigned long long* xlog_vals;
     unsigned long long xlog_cap;
     unsigned long long* xlog_count;
 };
 
-// Appends a removed term (the exact ledger sorts the log by rotation, then
-// key, before it sums: the reference's order).
+// Appends a removed term to the exact ledger's log.
 template <int W>
-__device__ __forceinline__ void log_removed(const HashArgs& a, unsigned r, const Key<W>& key,
-                                            double x) {
+__device__ __forceinline__ void log_removed(const HashArgs& a, const Key<W>& key, double x) {
     // one counter for the whole step: the threads that log together take
     // their positions with one atomic
     const cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
@@ -151,10 +151,7 @@ __device__ __forceinline__ void log_removed(const HashArgs& a, unsigned r, const
     if (g.thread_rank() == 0) pos = atomicAdd(a.xlog_count, (unsigned long long)g.size());
     pos = g.shfl(pos, 0) + g.thread_rank();
     if (pos >= a.xlog_cap) return;  // counted: the step reports the log full
-    uint64_t* k = a.xlog_keys + pos * (W + 1);
-#pragma unroll
-    for (int w = 0; w < W; ++w) k[w] = key.w[w];
-    k[W] = r;
+    store_key<W>(a.xlog_keys, pos, key);
     a.xlog_vals[pos] = abs_bits(x);
 }
 
@@ -615,7 +612,7 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
                     const unsigned long long out = settle<W>(p, E.key, from_bits(v), true, t);
                     if (out != v) store_val<W>(a.rec, E.slot, out);
                     if (a.xlog_keys && !out && !is_zero(from_bits(v)))
-                        log_removed<W>(a, r, E.key, from_bits(v));
+                        log_removed<W>(a, E.key, from_bits(v));
                 }
             }
         }
@@ -683,8 +680,8 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
                     const unsigned long long kbits = settle<W>(p, K, nk, k_live, t);
                     pbits = settle<W>(p, P, np, p_live, t);
                     if (a.xlog_keys) {
-                        if (!kbits && !is_zero(nk)) log_removed<W>(a, r, K, nk);
-                        if (!pbits && !is_zero(np)) log_removed<W>(a, r, P, np);
+                        if (!kbits && !is_zero(nk)) log_removed<W>(a, K, nk);
+                        if (!pbits && !is_zero(np)) log_removed<W>(a, P, np);
                     }
                     if (kbits != R.val) store_val<W>(a.rec, slot, kbits);
                     if (found >= 0) {
@@ -995,65 +992,356 @@ __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
     }
 }
 
-// Exact ledger: after the log is sorted by (rotation, key), one thread per
-// rotation finds its run and adds it in key order exactly as the reference's
-// merge loop does (tpgp_rev.c:716-729, upper_l2 :43-63 without MPFR):
-// l1 = upadd(l1, |v|), sq = upadd(sq, upmul(|v|, |v|)), l2 = nextUp(sqrt(sq)).
-// A log that overflowed reports ST_LOG (the host re-runs the step with a
-// larger one).
-template <int W>
-__global__ void __launch_bounds__(128) k_hash_xchains(HashArgs a, const uint64_t* keys,
-                                                     const unsigned long long* vals, HashRot* rot) {
-    const unsigned long long total = *a.xlog_count;
-    const unsigned r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (total > a.xlog_cap) {
-        if (r == 0) atomicOr(&a.st->status, ST_LOG);
-        return;
+// ---------------------------------------------------------------- exact ledger
+// The reference adds each rotation's removed |v| in key order as its merge
+// loop meets them (tpgp_rev.c:716-729; upper_l2 :43-63 without MPFR).  The
+// passes log them per rotation in any order, so after the passes:
+//   k_hash_xstarts: segment starts = exclusive scan of the removed counts;
+//   k_hash_xsort:   each segment sorted by key by one CTA (keys are unique
+//                   within a rotation: a key is in one pair per rotation);
+//   k_hash_xchains: one warp per rotation adds its segment sequentially.
+
+// One CTA of 1024 threads: starts[r] for r <= R; ST_LOG when the log
+// overflowed, ST_ORDER when the counts and the log disagree.  Clears the
+// sort's segment counter.
+__global__ void __launch_bounds__(1024) k_hash_xstarts(HashArgs a, const HashRot* rot,
+                                                       unsigned long long* starts,
+                                                       unsigned* next_segment) {
+    __shared__ unsigned long long s_part[32];
+    __shared__ unsigned long long s_carry;
+    const unsigned R = a.rotations, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) {
+        s_carry = 0ull;
+        *next_segment = 0u;
     }
-    if (r >= a.rotations) return;
-    // first entry of rotation r and of rotation r + 1 (the rotation is word W)
-    auto lower = [&](unsigned long long target) {
-        unsigned long long lo = 0, hi = total;
-        while (lo < hi) {
-            const unsigned long long mid = (lo + hi) / 2;
-            if (__ldcg(keys + mid * (W + 1) + W) < target) lo = mid + 1;
-            else hi = mid;
+    __syncthreads();
+    for (unsigned base = 0; base < R; base += 1024) {
+        const unsigned r = base + tid;
+        const unsigned long long mine = r < R ? rot[r].removed : 0ull;
+        unsigned long long incl = mine;  // warp inclusive scan
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= (unsigned)off) incl += y;
         }
-        return lo;
-    };
-    const unsigned long long b = lower(r), e = lower((unsigned long long)r + 1);
-    double l1 = 0.0, sq = 0.0;
-    for (unsigned long long k = b; k < e; ++k) {
-        const double v = from_bits(__ldcg(vals + k));
-        l1 = up_add(l1, v);
-        sq = up_add(sq, up_mul(v, v));
+        if (lane == 31) s_part[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = s_part[lane], wi = w;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, wi, off);
+                if (lane >= (unsigned)off) wi += y;
+            }
+            s_part[lane] = wi - w;  // exclusive warp offsets
+        }
+        __syncthreads();
+        if (r < R) starts[r] = s_carry + s_part[warp] + incl - mine;
+        __syncthreads();
+        if (tid == 1023) s_carry += s_part[31] + incl;  // chunk total (thread 1023 ends it)
+        __syncthreads();
     }
-    rot[r].l1 = l1;
-    rot[r].sq = sq;
-    rot[r].l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
+    if (tid == 0) {
+        starts[R] = s_carry;
+        const unsigned long long total = *a.xlog_count;
+        if (total > a.xlog_cap) atomicOr(&a.st->status, ST_LOG);
+        else if (total != s_carry) atomicOr(&a.st->status, ST_ORDER);
+    }
 }
 
-// One CTA.  Walks the rotations in order on one thread with the commit of
+// Segment sort: a stable LSD radix sort by key of each rotation's segment,
+// one CTA per segment (taken from a counter), on the onesweep tile scheme
+// without look-back (the CTA owns every tile of its segment, in order):
+// the histograms of all digits in one pass over the segment, then one
+// scatter pass per digit that is not constant over the segment, tile by
+// tile through shared memory, between the log's two halves.  A segment of
+// one tile stays in registers and shared memory for all its passes.  The
+// half that holds the sorted segment is noted in the rotation's HashRot.pad.
+template <int W>
+__host__ __device__ constexpr size_t xsort_smem() {
+    return (size_t)kOsTile * (8 * W + 8) + (size_t)8 * W * 256 * 4;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kOsBlock) k_hash_xsort(HashArgs a, const unsigned long long* starts,
+                                                         unsigned* next_segment, uint64_t* k1,
+                                                         unsigned long long* v1, HashRot* rot,
+                                                         int digits) {
+    extern __shared__ __align__(16) unsigned char xs_raw[];
+    uint64_t* st_k = reinterpret_cast<uint64_t*>(xs_raw);  // [tile][W]
+    unsigned long long* st_v = reinterpret_cast<unsigned long long*>(st_k + (size_t)kOsTile * W);
+    unsigned* s_h = reinterpret_cast<unsigned*>(st_v + kOsTile);  // [digit][256]: counts, then bases
+    __shared__ unsigned s_cnt[256], s_local[256], s_runt[256], s_run[256];
+    __shared__ unsigned s_w[kOsBlock / 32][256];
+    __shared__ unsigned s_part[kOsBlock / 32];
+    __shared__ unsigned s_seg, s_const;
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint64_t* const k0 = a.xlog_keys;
+    unsigned long long* const v0 = a.xlog_vals;
+    const int D = digits;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0)
+            s_seg = *reinterpret_cast<volatile unsigned*>(&a.st->status) ? a.rotations
+                                                                          : atomicAdd(next_segment, 1u);
+        __syncthreads();
+        const unsigned r = s_seg;
+        if (r >= a.rotations) return;
+        const unsigned long long b = starts[r];
+        const unsigned n = (unsigned)(starts[r + 1] - b);
+        if (n <= 1) {
+            if (tid == 0) rot[r].pad = 0u;  // in the log's first half already
+            continue;
+        }
+        // histograms of every digit over the segment
+        for (int q = tid; q < D * 256; q += kOsBlock) s_h[q] = 0u;
+        __syncthreads();
+        for (unsigned i = tid; i < n; i += kOsBlock) {
+            const Key<W> k = load_key<W>(k0, b + i);
+            for (int d = 0; d < D; ++d) atomicAdd(&s_h[d * 256 + sort_digit<W>(k, d)], 1u);
+        }
+        __syncthreads();
+        // exclusive bases per digit; a digit whose one bucket holds the whole
+        // segment is constant (its pass would not move anything): mark its
+        // bucket count as ~0u
+        for (int d = 0; d < D; ++d) {
+            const unsigned c = s_h[d * 256 + tid];
+            if (tid == 0) s_const = 0u;
+            __syncthreads();
+            if (c == n) s_const = 1u;
+            unsigned incl = c;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= (unsigned)off) incl += y;
+            }
+            if (lane == 31) s_part[warp] = incl;
+            __syncthreads();
+            unsigned before = 0;
+            for (unsigned w = 0; w < warp; ++w) before += s_part[w];
+            const bool skip = s_const != 0u;
+            __syncthreads();
+            s_h[d * 256 + tid] = skip ? ~0u : before + incl - c;
+        }
+        __syncthreads();
+        int half = 0;  // which half holds the segment's current order
+        if (n <= (unsigned)kOsTile) {
+            // one tile: registers and shared memory only
+            Key<W> key[kOsItems];
+            unsigned long long val[kOsItems];
+#pragma unroll
+            for (int e = 0; e < kOsItems; ++e) {
+                const unsigned i = (unsigned)e * kOsBlock + tid;
+                if (i < n) {
+                    key[e] = load_key<W>(k0, b + i);
+                    val[e] = __ldcg(v0 + b + i);
+                }
+            }
+            for (int d = 0; d < D; ++d) {
+                if (s_h[d * 256] == ~0u) continue;  // constant digit (uniform read)
+                unsigned dig[kOsItems];
+                s_cnt[tid] = 0u;
+                s_runt[tid] = 0u;
+                __syncthreads();
+#pragma unroll
+                for (int e = 0; e < kOsItems; ++e) {
+                    const unsigned i = (unsigned)e * kOsBlock + tid;
+                    dig[e] = i < n ? sort_digit<W>(key[e], d) : 256u;
+                }
+                // the tile's bucket offsets are the segment's bases
+#pragma unroll
+                for (int e = 0; e < kOsItems; ++e) {
+                    for (int q = lane; q < 256; q += 32) s_w[warp][q] = 0u;
+                    __syncthreads();
+                    const unsigned peers = __match_any_sync(0xffffffffu, dig[e]);
+                    if (dig[e] < 256u && lane == (unsigned)(__ffs(peers) - 1)) s_w[warp][dig[e]] = __popc(peers);
+                    __syncthreads();
+                    if (dig[e] < 256u) {
+                        unsigned bw = 0;
+                        for (unsigned w = 0; w < warp; ++w) bw += s_w[w][dig[e]];
+                        const unsigned pos = s_h[d * 256 + dig[e]] + s_runt[dig[e]] + bw +
+                                             __popc(peers & lanemask_lt());
+#pragma unroll
+                        for (int w = 0; w < W; ++w) st_k[(size_t)pos * W + w] = key[e].w[w];
+                        st_v[pos] = val[e];
+                    }
+                    __syncthreads();
+                    unsigned tot = 0;
+#pragma unroll
+                    for (int w = 0; w < kOsBlock / 32; ++w) tot += s_w[w][tid];
+                    s_runt[tid] += tot;
+                    __syncthreads();
+                }
+#pragma unroll
+                for (int e = 0; e < kOsItems; ++e) {
+                    const unsigned i = (unsigned)e * kOsBlock + tid;
+                    if (i < n) {
+#pragma unroll
+                        for (int w = 0; w < W; ++w) key[e].w[w] = st_k[(size_t)i * W + w];
+                        val[e] = st_v[i];
+                    }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int e = 0; e < kOsItems; ++e) {
+                const unsigned i = (unsigned)e * kOsBlock + tid;
+                if (i < n) {
+                    store_key<W>(k1, b + i, key[e]);
+                    v1[b + i] = val[e];
+                }
+            }
+            if (tid == 0) rot[r].pad = 1u;
+            continue;
+        }
+        for (int d = 0; d < D; ++d) {
+            if (s_h[d * 256] == ~0u) continue;  // constant digit
+            const uint64_t* sk = half ? k1 : k0;
+            const unsigned long long* sv = half ? v1 : v0;
+            uint64_t* dk = half ? k0 : k1;
+            unsigned long long* dv = half ? v0 : v1;
+            s_run[tid] = s_h[d * 256 + tid];  // where the bucket's next item goes
+            for (unsigned t0 = 0; t0 < n; t0 += kOsTile) {
+                __syncthreads();
+                s_cnt[tid] = 0u;
+                s_runt[tid] = 0u;
+                __syncthreads();
+                Key<W> key[kOsItems];
+                unsigned long long val[kOsItems];
+                unsigned dig[kOsItems];
+#pragma unroll
+                for (int e = 0; e < kOsItems; ++e) {
+                    const unsigned i = t0 + (unsigned)e * kOsBlock + tid;
+                    dig[e] = 256u;
+                    if (i < n) {
+                        key[e] = load_key<W>(sk, b + i);
+                        val[e] = __ldcg(sv + b + i);
+                        dig[e] = sort_digit<W>(key[e], d);
+                        atomicAdd(&s_cnt[dig[e]], 1u);
+                    }
+                }
+                __syncthreads();
+                {  // exclusive scan of the tile's counts
+                    const unsigned c = s_cnt[tid];
+                    unsigned incl = c;
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const unsigned y = __shfl_up_sync(0xffffffffu, incl, off);
+                        if (lane >= (unsigned)off) incl += y;
+                    }
+                    if (lane == 31) s_part[warp] = incl;
+                    __syncthreads();
+                    unsigned before = 0;
+                    for (unsigned w = 0; w < warp; ++w) before += s_part[w];
+                    s_local[tid] = before + incl - c;
+                }
+#pragma unroll
+                for (int e = 0; e < kOsItems; ++e) {
+                    for (int q = lane; q < 256; q += 32) s_w[warp][q] = 0u;
+                    __syncthreads();
+                    const unsigned peers = __match_any_sync(0xffffffffu, dig[e]);
+                    if (dig[e] < 256u && lane == (unsigned)(__ffs(peers) - 1)) s_w[warp][dig[e]] = __popc(peers);
+                    __syncthreads();
+                    if (dig[e] < 256u) {
+                        unsigned bw = 0;
+                        for (unsigned w = 0; w < warp; ++w) bw += s_w[w][dig[e]];
+                        const unsigned pos = s_local[dig[e]] + s_runt[dig[e]] + bw + __popc(peers & lanemask_lt());
+#pragma unroll
+                        for (int w = 0; w < W; ++w) st_k[(size_t)pos * W + w] = key[e].w[w];
+                        st_v[pos] = val[e];
+                    }
+                    __syncthreads();
+                    unsigned tot = 0;
+#pragma unroll
+                    for (int w = 0; w < kOsBlock / 32; ++w) tot += s_w[w][tid];
+                    s_runt[tid] += tot;
+                    __syncthreads();
+                }
+                // write out: a bucket's run of the tile to consecutive addresses
+                const unsigned len = min((unsigned)kOsTile, n - t0);
+                for (unsigned q = tid; q < len; q += kOsBlock) {
+                    Key<W> k;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) k.w[w] = st_k[(size_t)q * W + w];
+                    const unsigned bk = sort_digit<W>(k, d);
+                    const unsigned long long to = b + s_run[bk] + (q - s_local[bk]);
+                    store_key<W>(dk, to, k);
+                    dv[to] = st_v[q];
+                }
+                __syncthreads();
+                s_run[tid] += s_cnt[tid];
+            }
+            __syncthreads();
+            half ^= 1;
+        }
+        if (tid == 0) rot[r].pad = (unsigned)half;
+    }
+}
+
+// One warp per rotation: the sorted segment's values added in order, 32 at
+// a time by warp_up_sum (bit for bit the sequential chain of the sorted
+// kernels' k_exact_chains), the loads of the next 256 in flight meanwhile.
+__global__ void __launch_bounds__(256) k_hash_xchains(HashArgs a, const unsigned long long* v1,
+                                                      const unsigned long long* starts, HashRot* rot) {
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const unsigned r = blockIdx.x * 8u + warp;
+    if (r >= a.rotations || *reinterpret_cast<volatile unsigned*>(&a.st->status)) return;
+    const unsigned long long b = starts[r], e = starts[r + 1];
+    const unsigned long long* vals = rot[r].pad ? v1 : a.xlog_vals;
+    double l1 = 0.0, sq = 0.0;
+    unsigned long long nxt[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const unsigned long long i = b + (unsigned long long)q * 32 + lane;
+        nxt[q] = i < e ? __ldcg(vals + i) : 0ull;
+    }
+    for (unsigned long long c = b; c < e; c += 256) {
+        unsigned long long cur[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            cur[q] = nxt[q];
+            const unsigned long long i = c + 256 + (unsigned long long)q * 32 + lane;
+            nxt[q] = i < e ? __ldcg(vals + i) : 0ull;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            if (c + (unsigned long long)q * 32 >= e) break;  // warp-uniform
+            const bool has = c + (unsigned long long)q * 32 + lane < e;
+            const double v = from_bits(cur[q]);
+            l1 = warp_up_sum(l1, v, has, nullptr);
+            sq = warp_up_sum(sq, has ? up_mul(v, v) : 0.0, has, nullptr);
+        }
+    }
+    if (lane == 0) {
+        rot[r].l1 = l1;
+        rot[r].sq = sq;
+        rot[r].l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
+    }
+}
+
+// One CTA.  Commits the rotations in order with the checks of
 // commit_rotation: table overflow, ENUMERIC (nonfinite merged values), ECAP,
-// ledger update, ENUMERIC (ledger), EBUDGET; an empty map is a no-op rotation
-// (no ledger change).  The records are staged through shared memory in
-// chunks so the sequential walk never waits on global memory.  Writes n,
-// ledger, terms_in and status.
+// ledger update, ENUMERIC (ledger), EBUDGET; an empty map is a no-op
+// rotation (no ledger change).  The records are staged through shared
+// memory in chunks; warp 0 takes them 32 at a time: the term counts by a
+// warp scan, the ledger's upward sums by warp_up_sum (the sequential
+// chain's bits), each lane's checks on its own prefix, and the rotations
+// before the first failing lane commit.  Writes n, ledger, terms_in and status.
 constexpr int kChainChunk = 512;
 __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* rot) {
     __shared__ HashRot s_rot[kChainChunk];
     __shared__ int s_stop;
-    const unsigned R = a.rotations;
+    const unsigned R = a.rotations, lane = threadIdx.x & 31u;
     DeviceState* st = a.st;
     unsigned status = 0;
     unsigned long long n = 0, terms = 0, done = 0;
     Ledger led;
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
         status = st->status;
         n = st->n;
         led = st->ledger;
-        s_stop = status != 0;
     }
+    if (threadIdx.x == 0) s_stop = status != 0;
     const RotParams& p0 = a.ps[0];  // a step's rotations share their options
     for (unsigned base = 0; base < R; base += kChainChunk) {
         __syncthreads();
@@ -1061,53 +1349,67 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
         const unsigned cnt = min((unsigned)kChainChunk, R - base);
         for (unsigned k = threadIdx.x; k < cnt; k += blockDim.x) s_rot[k] = rot[base + k];
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (unsigned k = 0; k < cnt && !status; ++k) {
-                const HashRot& h = s_rot[k];
-                if (h.flags & ST_TABLE) {
-                    status = ST_TABLE;
-                    break;
+        if (threadIdx.x < 32) {
+            for (unsigned g = 0; g < cnt && !status; g += 32) {
+                const unsigned k = g + lane;
+                const bool valid = k < cnt;
+                HashRot h{};
+                if (valid) h = s_rot[k];
+                // terms before and after this rotation
+                long long incl = valid ? h.dn : 0ll;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const long long y = __shfl_up_sync(0xffffffffu, incl, off);
+                    if (lane >= (unsigned)off) incl += y;
                 }
-                if (__ldcg(&st->status) & ST_LOG) {  // exact-ledger log too small
-                    status = ST_LOG;
-                    break;
+                const unsigned long long nb = (unsigned long long)((long long)n + incl - h.dn);
+                const unsigned long long no = (unsigned long long)((long long)n + incl);
+                const bool live = valid && nb != 0;  // an empty map's rotation is a no-op
+                double l1i, l2i, sqi;
+                warp_up_sum(led.dropped_l1, h.l1, live, &l1i);
+                warp_up_sum(led.dropped_l2, h.l2, live, &l2i);
+                warp_up_sum(led.dropped_l2_squared, h.sq, live, &sqi);
+                unsigned f = 0;  // this rotation's failure, in the checks' order
+                if (valid) {
+                    if (h.flags & ST_TABLE) f = ST_TABLE;
+                    else if (h.flags & ST_NUMERIC) f = ST_NUMERIC;
+                    else if (!live && h.dn != 0) f = ST_ORDER;  // an empty map cannot gain terms
+                    else if (live) {
+                        if (p0.max_terms && no > p0.max_terms) f = ST_CAP;
+                        else if (!is_finite(l2i) || !is_finite(led.arithmetic_l2)) f = ST_NUMERIC;
+                        else if (p0.max_drop_l2 != 0.0 && l2i > p0.max_drop_l2) f = ST_BUDGET;
+                    }
                 }
-                if (h.flags & ST_NUMERIC) {
-                    status = ST_NUMERIC;
-                    break;
+                const unsigned fm = __ballot_sync(0xffffffffu, f != 0);
+                const unsigned F = fm ? (unsigned)(__ffs(fm) - 1) : 32u;
+                const bool commit = valid && lane < F;
+                const unsigned cm = __ballot_sync(0xffffffffu, commit);
+                const unsigned lm = __ballot_sync(0xffffffffu, commit && live);
+                const unsigned rm = __ballot_sync(0xffffffffu, commit && live && h.removed != 0);
+                unsigned long long add = commit ? nb : 0ull, peak = commit && live ? no : 0ull;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    add += __shfl_xor_sync(0xffffffffu, add, off);
+                    peak = max(peak, __shfl_xor_sync(0xffffffffu, peak, off));
                 }
-                if (n == 0) {  // empty map: the rotation is a no-op
-                    ++done;
-                    continue;
+                if (cm) {
+                    n = __shfl_sync(0xffffffffu, no, 31 - __clz(cm));
+                    terms += add;
+                    done += __popc(cm);
                 }
-                const unsigned long long n_out = (unsigned long long)((long long)n + h.dn);
-                if (p0.max_terms && n_out > p0.max_terms) {
-                    status = ST_CAP;
-                    break;
+                if (lm) {
+                    const unsigned ll = 31 - __clz(lm);
+                    led.dropped_l1 = __shfl_sync(0xffffffffu, l1i, ll);
+                    led.dropped_l2 = __shfl_sync(0xffffffffu, l2i, ll);
+                    led.dropped_l2_squared = __shfl_sync(0xffffffffu, sqi, ll);
+                    led.rotations += __popc(lm);
+                    led.removal_events += __popc(rm);
+                    if (peak > led.peak_terms) led.peak_terms = peak;
+                    led.arithmetic_enclosed = 0;
                 }
-                Ledger next = led;
-                next.dropped_l1 = up_add(next.dropped_l1, h.l1);
-                next.dropped_l2 = up_add(next.dropped_l2, h.l2);
-                next.dropped_l2_squared = up_add(next.dropped_l2_squared, h.sq);
-                next.arithmetic_l2 = up_add(next.arithmetic_l2, 0.0);
-                next.rotations += 1;
-                if (h.removed) next.removal_events += 1;
-                if (n_out > next.peak_terms) next.peak_terms = n_out;
-                next.arithmetic_enclosed = 0;
-                if (!is_finite(next.dropped_l2) || !is_finite(next.arithmetic_l2)) {
-                    status = ST_NUMERIC;
-                    break;
-                }
-                if (p0.max_drop_l2 != 0.0 && next.dropped_l2 > p0.max_drop_l2) {
-                    status = ST_BUDGET;
-                    break;
-                }
-                led = next;
-                terms += n;
-                n = n_out;
-                ++done;
+                if (fm) status = __shfl_sync(0xffffffffu, f, F);
             }
-            s_stop = status != 0;
+            if (threadIdx.x == 0) s_stop = status != 0;
         }
     }
     if (threadIdx.x != 0) return;

@@ -34,6 +34,25 @@ def evolve(hash_on, n, keys, vals, terms, dt, steps, opts, ledger=None):
 
 
 @pytest.mark.parametrize("n_spins", [24, 60, 90, 120])
+def test_exact_ledger_hash_matches_sorted(n_spins):
+    """The exact ledger through the hash-table step (removed terms logged,
+    sorted per rotation, added in key order) against the sorted kernels'
+    in-order sums, W = 1..4: maps, FIDs and every ledger field bitwise."""
+    rng = np.random.default_rng(100 + n_spins)
+    keys, vals = random_map(rng, n_spins, 3000)
+    terms = H.ring_j1j2(n_spins, 1.0, 0.3)
+    opts = options(1e-3, exact_ledger=True)
+    a = evolve(True, n_spins, keys, vals, terms, 0.03, 3, opts)
+    b = evolve(False, n_spins, keys, vals, terms, 0.03, 3, opts)
+    assert a[0] == b[0] == 0, (a[5], b[5])
+    assert a[4].removal_events > 0
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(bits(a[2]), bits(b[2]))
+    assert np.array_equal(bits(a[3]), bits(b[3]))
+    assert np.array_equal(bits(ledger_vec(a[4])), bits(ledger_vec(b[4])))
+
+
+@pytest.mark.parametrize("n_spins", [24, 60, 90, 120])
 def test_hash_matches_sorted_random_maps(n_spins):
     """Random multi-site maps (W = 1..4) under three steps of a ring with
     next-nearest couplings: hash and sorted paths bitwise equal."""
