@@ -120,6 +120,18 @@ class Engine:
                 raise ValueError(f"upload failed ({STATUS_NAMES[st]}): {msg}")
         return m
 
+    def upward_sums(self, x, chain):
+        """Upward sums of consecutive chains of `chain` addends on the device
+        (tpgp_gb_upward_sums): bit for bit the sequential upadd chain."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(max(0, -(-len(x) // chain)), dtype=np.float64)
+        f64p = C.POINTER(C.c_double)
+        st = self.lib.tpgp_gb_upward_sums(self.ptr, x.ctypes.data_as(f64p), len(x), chain,
+                                          out.ctypes.data_as(f64p))
+        if st:
+            raise RuntimeError(f"tpgp_gb_upward_sums failed ({STATUS_NAMES[st]})")
+        return out
+
     def serve(self, requests, slots=(8, 8, 8), memory_budget=64 << 30, record_fid=True):
         """Serves FID-solve requests with continuous batching (tpgp_gb_serve).
 

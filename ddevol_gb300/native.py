@@ -141,6 +141,8 @@ def _bind(lib):
     lib.tpgp_gb_checkpoint_free.argtypes = [P(GbCheckpoint)]
     lib.tpgp_gb_map_l2.restype = C.c_int
     lib.tpgp_gb_map_l2.argtypes = [C.c_void_p, f64p]
+    lib.tpgp_gb_upward_sums.restype = C.c_int
+    lib.tpgp_gb_upward_sums.argtypes = [C.c_void_p, f64p, C.c_size_t, C.c_size_t, f64p]
     lib.tpgp_gb_strang_bound.restype = C.c_double
     lib.tpgp_gb_strang_bound.argtypes = [P(GbTerm), sz, C.c_double]
     lib.tpgp_gb_liouvillian.restype = C.c_int

@@ -192,6 +192,16 @@ tpgp_gb_status tpgp_gb_checkpoint_save(const char *path, const tpgp_gb_map *map,
  * (engine/include/tpgp_rev.h:75, engine/src/tpgp_rev.c:266-271). */
 tpgp_gb_status tpgp_gb_map_l2(const tpgp_gb_map *map, double *l2);
 
+/* Upward sums of consecutive chains of `chain` addends (the last one may be
+ * shorter): out[c] = upadd(...upadd(upadd(0, x[c*chain]), x[c*chain+1])...),
+ * upadd(a, b) = nextafter(a + b, +inf) with a zero operand returning the
+ * other (engine/src/tpgp_rev.c:25-36), bit for bit the sequential chain;
+ * addends >= 0.  The device kernel behind the exact ledger's per-rotation
+ * sums and the step's ledger commit, computed by a warp 32 addends at a time.
+ * out holds ceil(n / chain) values. */
+tpgp_gb_status tpgp_gb_upward_sums(tpgp_gb_context *context, const double *x, size_t n,
+                                   size_t chain, double *out);
+
 /* Conservative third-order Strang bound per step for the ordered terms,
  * bitwise equal to tpgp_strang_bound (engine/include/tpgp_rev.h:91-94,
  * engine/src/tpgp_rev.c:887-961); NaN for an invalid term list.  Host
