@@ -371,6 +371,19 @@ def run_gb300(args, dist):
         m, terms, led, step0 = prepare_state(eng, cfg, args.target_terms, args.max_setup_steps, opts)
         k_win, v_win = m.download()
         start = {"setup_steps": step0, "setup_target_terms": args.target_terms}
+    # the engine's launch configuration for this workload: one timed step per
+    # candidate from the start state (kept), the fastest applied (before the
+    # warm-up; the e2e leg steps the same map)
+    tuning = None
+    if not args.no_autotune:
+        t = m.autotune(terms, cfg["dt"], opts)
+        name = lambda c: (f"hash ctas={c['hash_ctas']} pdl={c['hash_pdl']} fuse={c['hash_fuse']}"
+                          if c["hash_step"] else f"sorted pdl={c['sorted_pdl']}")
+        tuning = {"chosen": name(t["chosen"]), "chosen_ms": round(t["chosen"]["step_ms"], 3),
+                  "default": name(t["before"]), "default_ms": round(t["before"]["step_ms"], 3),
+                  "tried_ms": {name(c): round(c["step_ms"], 3) for c in t["tried"][1:]},
+                  "basis": "device time of one Strang step from the start state per candidate, "
+                           "after one untimed step"}
     # With the hash-table step the per-phase CUDA events are part of each
     # step's graph, so the dominant kernel's launch time is measured on the
     # timed steps themselves; the warm-up steps capture that same graph.
@@ -538,6 +551,7 @@ def run_gb300(args, dist):
             "kernel_ms": {k2: round(v2[0], 3) for k2, v2 in prof.items()}},
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "engine_tuning": tuning,
         "fid_last": float(fids[-1]) if len(fids) else None,
         "forms": forms,
         "libraries": repo_libraries(),
@@ -969,6 +983,8 @@ def main():
     ap.add_argument("--max-setup-steps", type=int, default=400)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the engine's default launch configuration (no tpgp_gb_map_autotune)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the plain-solve, exact-ledger, powder and serving sub-lines")
     ap.add_argument("--form-seconds", type=float, default=15.0,

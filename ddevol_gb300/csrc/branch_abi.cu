@@ -38,14 +38,7 @@ static_assert(sizeof(double) == 8 && DBL_MANT_DIG == 53 && FLT_RADIX == 2,
 
 namespace {
 
-// Largest |x - neighbour| over the two adjacent binary64 values: the
-// rounding radius of the serial engine (engine/src/tpgp_rev.c:37-42).
-__device__ __forceinline__ double rounding_radius(double x) {
-    if (!tg::is_finite(x)) return __longlong_as_double(0x7ff0000000000000ll);
-    const double up = tg::next_up(x), down = tg::negate(tg::next_up(tg::negate(x)));
-    const double a = fabs(__dsub_rn(up, x)), b = fabs(__dsub_rn(x, down));
-    return a > b ? a : b;
-}
+using tg::rounding_radius;  // the serial engine's round_radius (engine/src/tpgp_rev.c:37-42)
 
 // W > 0: keys of exactly W words held in registers; W == 0: any word count.
 template <int W>

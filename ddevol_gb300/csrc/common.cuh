@@ -256,6 +256,15 @@ __device__ __forceinline__ double up_mul(double a, double b) {
     return next_up(__dmul_rn(a, b));
 }
 
+// Largest |x - neighbour| over the two adjacent binary64 values, +inf for a
+// nonfinite x: round_radius of engine/src/tpgp_rev.c:37-42.
+__device__ __forceinline__ double rounding_radius(double x) {
+    if (!is_finite(x)) return from_bits(kExpMask);
+    const double up = next_up(x), down = negate(next_up(negate(x)));
+    const double a = abs_of(__dsub_rn(up, x)), b = abs_of(__dsub_rn(x, down));
+    return a > b ? a : b;
+}
+
 // A chain of up_add over the lanes' addends, in lane order, computed by the
 // warp together with the same result bits as the sequential chain:
 // returns up_add(...up_add(up_add(s, x_0), x_1)..., x_31) over the lanes

@@ -64,7 +64,8 @@ struct HashStat {
     unsigned long long l1[4], sq[4];
     unsigned long long born, died, removed;
     unsigned int flags, pad;
-    unsigned long long unused[4];
+    unsigned long long radii;  // merged radii logged (validated rotations)
+    unsigned long long unused[3];
 };
 static_assert(sizeof(HashStat) == 128, "stat slot is two 64-byte lines");
 
@@ -86,6 +87,8 @@ struct PassParams {
     unsigned long long threshold_bits;
     uint64_t mask[4];
     int fx_unit1, fx_unit2;
+    unsigned validated;  // children carry error radii (rc, rs)
+    double rc, rs;
 };
 
 __host__ __device__ inline PassParams pass_params(const RotParams& r) {
@@ -113,6 +116,9 @@ __host__ __device__ inline PassParams pass_params(const RotParams& r) {
     for (int w = 0; w < 4; ++w) p.mask[w] = r.mask[w];
     p.fx_unit1 = r.fx_unit1;
     p.fx_unit2 = r.fx_unit2;
+    p.validated = r.validated ? 1u : 0u;
+    p.rc = r.rc;
+    p.rs = r.rs;
     return p;
 }
 
@@ -141,9 +147,11 @@ struct HashArgs {
     unsigned long long* xlog_count;
 };
 
-// Appends a removed term to the exact ledger's log.
+// Appends an entry to the exact ledger's log: a removed term's |v| bits, or
+// (sign bit set) a validated rotation's merged radius of the key.
 template <int W>
-__device__ __forceinline__ void log_removed(const HashArgs& a, const Key<W>& key, double x) {
+__device__ __forceinline__ void log_entry(const HashArgs& a, const Key<W>& key,
+                                          unsigned long long bits) {
     // one counter for the whole step: the threads that log together take
     // their positions with one atomic
     const cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
@@ -152,8 +160,13 @@ __device__ __forceinline__ void log_removed(const HashArgs& a, const Key<W>& key
     pos = g.shfl(pos, 0) + g.thread_rank();
     if (pos >= a.xlog_cap) return;  // counted: the step reports the log full
     store_key<W>(a.xlog_keys, pos, key);
-    a.xlog_vals[pos] = abs_bits(x);
+    a.xlog_vals[pos] = bits;
 }
+template <int W>
+__device__ __forceinline__ void log_removed(const HashArgs& a, const Key<W>& key, double x) {
+    log_entry<W>(a, key, abs_bits(x));
+}
+
 
 // Record layout: words 0..W-1 the key, word W the value bits, the low half
 // of word W+1 the tag.
@@ -422,12 +435,13 @@ __global__ void __launch_bounds__(kHashBlock) k_hash_build(HashArgs a) {
 // shared or global atomic while it removes terms.
 struct PairTally {
     unsigned born, died, removed, flags;
+    unsigned radii;
     U128 l1, sq;
 };
 
 __device__ __forceinline__ PairTally empty_tally() {
     PairTally t;
-    t.born = t.died = t.removed = t.flags = 0u;
+    t.born = t.died = t.removed = t.flags = t.radii = 0u;
     t.l1 = U128{0ull, 0ull};
     t.sq = U128{0ull, 0ull};
     return t;
@@ -512,6 +526,7 @@ __device__ __forceinline__ void warp_tally(PairTally& t) {
     t.born = __reduce_add_sync(0xffffffffu, t.born);
     t.died = __reduce_add_sync(0xffffffffu, t.died);
     t.flags = __reduce_or_sync(0xffffffffu, t.flags);
+    t.radii = __reduce_add_sync(0xffffffffu, t.radii);
     if (__any_sync(0xffffffffu, t.removed != 0u)) {
         t.removed = __reduce_add_sync(0xffffffffu, t.removed);
         t.l1 = warp_sum_u128(t.l1);
@@ -527,13 +542,14 @@ __device__ __forceinline__ void flush_tally(const HashArgs& a, unsigned r, PairT
     if (lane == 0) s_t[warp] = t;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long born = 0, died = 0, removed = 0;
+        unsigned long long born = 0, died = 0, removed = 0, radii = 0;
         unsigned flags = 0;
         U128 l1{0ull, 0ull}, sq{0ull, 0ull};
         for (int w = 0; w < NT / 32; ++w) {
             born += s_t[w].born;
             died += s_t[w].died;
             removed += s_t[w].removed;
+            radii += s_t[w].radii;
             flags |= s_t[w].flags;
             u128_add(l1, s_t[w].l1);
             u128_add(sq, s_t[w].sq);
@@ -544,7 +560,60 @@ __device__ __forceinline__ void flush_tally(const HashArgs& a, unsigned r, PairT
         if (born) atomicAdd(&hs->born, born);
         if (died) atomicAdd(&hs->died, died);
         if (removed) atomicAdd(&hs->removed, removed);
+        if (radii) atomicAdd(&hs->radii, radii);
         if (flags) atomicOr(&hs->flags, flags);
+    }
+}
+
+// Validated rotation: the merged radii of a pair's two output keys
+// (tpgp_rev.c:459-464 per child, :699-706 per merge).  Each live member
+// sends a cos child to itself with radius upadd(upmul(|v|, rc),
+// round_radius(v c)) and a sin child to its partner with radius
+// upadd(upmul(|v|, rs), round_radius(v s)); a key's radius is the upadd of
+// its contributions' radii and, where two nonzero contributions meet, the
+// rounding radius of their sum.  Nonzero merged radii are logged (tagged);
+// a nonfinite child or merged radius is ENUMERIC.
+template <int W>
+__device__ __forceinline__ void pair_radii(const HashArgs& a, const PassParams& p, const Key<W>& K,
+                                           const Key<W>& P, bool k_live, bool p_live, double vk,
+                                           double vp, double nk, double np, PairTally& t) {
+    double kc = 0.0, ks = 0.0, pc = 0.0, ps = 0.0;  // child radii: K's cos / sin, P's cos / sin
+    double xk = 0.0, yk = 0.0, xp = 0.0, yp = 0.0;  // the children's values (before signs)
+    if (k_live) {
+        xk = __dmul_rn(vk, p.c);
+        yk = __dmul_rn(vk, p.s);
+        kc = up_add(up_mul(abs_of(vk), p.rc), rounding_radius(xk));
+        ks = up_add(up_mul(abs_of(vk), p.rs), rounding_radius(yk));
+    }
+    if (p_live) {
+        xp = __dmul_rn(vp, p.c);
+        yp = __dmul_rn(vp, p.s);
+        pc = up_add(up_mul(abs_of(vp), p.rc), rounding_radius(xp));
+        ps = up_add(up_mul(abs_of(vp), p.rs), rounding_radius(yp));
+    }
+    double rk, rp;
+    if (k_live && p_live) {
+        rk = up_add(kc, ps);
+        if (!is_zero(xk) && !is_zero(yp)) rk = up_add(rk, rounding_radius(nk));
+        rp = up_add(pc, ks);
+        if (!is_zero(xp) && !is_zero(yk)) rp = up_add(rp, rounding_radius(np));
+    } else if (k_live) {
+        rk = kc;
+        rp = ks;
+    } else {
+        rk = ps;
+        rp = pc;
+    }
+    if (!is_finite(kc) || !is_finite(ks) || !is_finite(pc) || !is_finite(ps) || !is_finite(rk) ||
+        !is_finite(rp))
+        t.flags |= ST_NUMERIC;
+    if (!is_zero(rk)) {
+        log_entry<W>(a, K, dbits(rk) | kSignBit);
+        ++t.radii;
+    }
+    if (!is_zero(rp)) {
+        log_entry<W>(a, P, dbits(rp) | kSignBit);
+        ++t.radii;
     }
 }
 
@@ -570,7 +639,9 @@ __device__ __forceinline__ unsigned pass_index(const PassParams& p, const Key<W>
 // The first round's entries are loaded without waiting for the list length:
 // entries past the length are unwritten (the list starts filled with all
 // ones), and entries appended by this pass carry this pass's stamp.
-template <int W, int NT>
+// V: validated rotations (error radii), a separate instantiation so the
+// plain pass keeps its registers.
+template <int W, int NT, bool V = false>
 __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p, unsigned r,
                                           unsigned k) {
     __shared__ PairTally s_t[NT / 32];
@@ -679,6 +750,8 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
                     }
                     const unsigned long long kbits = settle<W>(p, K, nk, k_live, t);
                     pbits = settle<W>(p, P, np, p_live, t);
+                    if constexpr (V)
+                        pair_radii<W>(a, p, K, P, k_live, p_live, from_bits(R.val), from_bits(pb), nk, np, t);
                     if (a.xlog_keys) {
                         if (!kbits && !is_zero(nk)) log_removed<W>(a, K, nk);
                         if (!pbits && !is_zero(np)) log_removed<W>(a, P, np);
@@ -730,11 +803,11 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
 // Launched with programmatic stream serialization (hash_pdl), a pass's CTAs
 // become resident while the previous pass drains and wait here for its
 // completion and memory; launched plainly, pdl_enter returns at once.
-template <int W>
+template <int W, bool V = false>
 __global__ void __launch_bounds__(kHashBlock, 4) k_hash_rotate(HashArgs a, PassParams p, unsigned r,
                                                                unsigned k) {
     pdl_enter();
-    hash_pass<W, kHashBlock>(a, p, r, k);
+    hash_pass<W, kHashBlock, V>(a, p, r, k);
 }
 
 // All rotations of a step in one cooperative launch (one CTA of 1024 threads
@@ -959,7 +1032,9 @@ struct HashRot {
     double l1, sq, l2;
     long long dn;                  // born - died
     unsigned long long removed;
-    unsigned flags, pad;
+    unsigned flags, pad;           // pad: the exact ledger's sort notes its result half here
+    unsigned long long radii;      // merged radii logged (validated rotations)
+    double ar;                     // upper L2 of the merged radii (validated rotations)
 };
 
 __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
@@ -967,7 +1042,7 @@ __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
     if (r >= a.rotations) return;
     const HashStat& x = a.stats[(size_t)r * kStatSlots + lane];
     U128 l1 = limbs_total(x.l1), sq = limbs_total(x.sq);
-    unsigned long long born = x.born, died = x.died, removed = x.removed;
+    unsigned long long born = x.born, died = x.died, removed = x.removed, radii = x.radii;
     unsigned flags = x.flags;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -976,6 +1051,7 @@ __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
         born += __shfl_down_sync(0xffffffffu, born, off);
         died += __shfl_down_sync(0xffffffffu, died, off);
         removed += __shfl_down_sync(0xffffffffu, removed, off);
+        radii += __shfl_down_sync(0xffffffffu, radii, off);
         flags |= __shfl_down_sync(0xffffffffu, flags, off);
     }
     if (lane == 0) {
@@ -988,6 +1064,8 @@ __global__ void __launch_bounds__(256) k_hash_reduce(HashArgs a, HashRot* rot) {
         h.removed = removed;
         h.flags = flags;
         h.pad = 0;
+        h.radii = radii;
+        h.ar = 0.0;
         rot[r] = h;
     }
 }
@@ -1017,7 +1095,7 @@ __global__ void __launch_bounds__(1024) k_hash_xstarts(HashArgs a, const HashRot
     __syncthreads();
     for (unsigned base = 0; base < R; base += 1024) {
         const unsigned r = base + tid;
-        const unsigned long long mine = r < R ? rot[r].removed : 0ull;
+        const unsigned long long mine = r < R ? rot[r].removed + rot[r].radii : 0ull;
         unsigned long long incl = mine;  // warp inclusive scan
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
@@ -1278,9 +1356,12 @@ __global__ void __launch_bounds__(kOsBlock) k_hash_xsort(HashArgs a, const unsig
     }
 }
 
-// One warp per rotation: the sorted segment's values added in order, 32 at
-// a time by warp_up_sum (bit for bit the sequential chain of the sorted
-// kernels' k_exact_chains), the loads of the next 256 in flight meanwhile.
+// One warp per rotation: the sorted segment's entries added in key order,
+// 32 at a time by warp_up_sum (bit for bit the sequential chains of the
+// sorted kernels' k_exact_chains), the loads of the next 256 in flight
+// meanwhile: the removed |v| into l1 and l2-squared, and (validated
+// rotations, sign-tagged entries) the merged radii into arithmetic_l2's
+// upper L2 (tpgp_rev.c:734-738 with the non-MPFR upper_l2, :57-62).
 __global__ void __launch_bounds__(256) k_hash_xchains(HashArgs a, const unsigned long long* v1,
                                                       const unsigned long long* starts, HashRot* rot) {
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -1288,7 +1369,8 @@ __global__ void __launch_bounds__(256) k_hash_xchains(HashArgs a, const unsigned
     if (r >= a.rotations || *reinterpret_cast<volatile unsigned*>(&a.st->status)) return;
     const unsigned long long b = starts[r], e = starts[r + 1];
     const unsigned long long* vals = rot[r].pad ? v1 : a.xlog_vals;
-    double l1 = 0.0, sq = 0.0;
+    const bool radii = rot[r].radii != 0;  // warp-uniform
+    double l1 = 0.0, sq = 0.0, ar = 0.0;
     unsigned long long nxt[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -1307,15 +1389,19 @@ __global__ void __launch_bounds__(256) k_hash_xchains(HashArgs a, const unsigned
         for (int q = 0; q < 8; ++q) {
             if (c + (unsigned long long)q * 32 >= e) break;  // warp-uniform
             const bool has = c + (unsigned long long)q * 32 + lane < e;
-            const double v = from_bits(cur[q]);
-            l1 = warp_up_sum(l1, v, has, nullptr);
-            sq = warp_up_sum(sq, has ? up_mul(v, v) : 0.0, has, nullptr);
+            const bool tag = (cur[q] >> 63) != 0ull;
+            const double v = from_bits(cur[q] & ~kSignBit);
+            const bool rem = has && !tag;
+            l1 = warp_up_sum(l1, rem ? v : 0.0, rem, nullptr);
+            sq = warp_up_sum(sq, rem ? up_mul(v, v) : 0.0, rem, nullptr);
+            if (radii) ar = warp_up_sum(ar, has && tag ? up_mul(v, v) : 0.0, has && tag, nullptr);
         }
     }
     if (lane == 0) {
         rot[r].l1 = l1;
         rot[r].sq = sq;
         rot[r].l2 = sq == 0.0 ? 0.0 : next_up(sqrt(sq));
+        rot[r].ar = ar == 0.0 ? 0.0 : next_up(sqrt(ar));
     }
 }
 
@@ -1365,10 +1451,11 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
                 const unsigned long long nb = (unsigned long long)((long long)n + incl - h.dn);
                 const unsigned long long no = (unsigned long long)((long long)n + incl);
                 const bool live = valid && nb != 0;  // an empty map's rotation is a no-op
-                double l1i, l2i, sqi;
+                double l1i, l2i, sqi, ari;
                 warp_up_sum(led.dropped_l1, h.l1, live, &l1i);
                 warp_up_sum(led.dropped_l2, h.l2, live, &l2i);
                 warp_up_sum(led.dropped_l2_squared, h.sq, live, &sqi);
+                warp_up_sum(led.arithmetic_l2, h.ar, live, &ari);  // 0 unless validated
                 unsigned f = 0;  // this rotation's failure, in the checks' order
                 if (valid) {
                     if (h.flags & ST_TABLE) f = ST_TABLE;
@@ -1376,7 +1463,7 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
                     else if (!live && h.dn != 0) f = ST_ORDER;  // an empty map cannot gain terms
                     else if (live) {
                         if (p0.max_terms && no > p0.max_terms) f = ST_CAP;
-                        else if (!is_finite(l2i) || !is_finite(led.arithmetic_l2)) f = ST_NUMERIC;
+                        else if (!is_finite(l2i) || !is_finite(ari)) f = ST_NUMERIC;
                         else if (p0.max_drop_l2 != 0.0 && l2i > p0.max_drop_l2) f = ST_BUDGET;
                     }
                 }
@@ -1402,6 +1489,7 @@ __global__ void __launch_bounds__(256) k_hash_chain(HashArgs a, const HashRot* r
                     led.dropped_l1 = __shfl_sync(0xffffffffu, l1i, ll);
                     led.dropped_l2 = __shfl_sync(0xffffffffu, l2i, ll);
                     led.dropped_l2_squared = __shfl_sync(0xffffffffu, sqi, ll);
+                    led.arithmetic_l2 = __shfl_sync(0xffffffffu, ari, ll);
                     led.rotations += __popc(lm);
                     led.removal_events += __popc(rm);
                     if (peak > led.peak_terms) led.peak_terms = peak;

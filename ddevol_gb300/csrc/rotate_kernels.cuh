@@ -57,6 +57,8 @@ struct RotParams {
     int th[8];              // threshold bit positions
     int lev_lo[4], lev_hi[4];  // index in th of mbit[l] and mbit[l] + 1
     int exact_ledger;       // 1: removed values kept in order for a sequential ledger
+    int validated;          // 1: children carry error radii from rc, rs (hash-table step only)
+    double rc, rs;          // radii of c and s (validated)
     unsigned wait_polls;    // device waits give up after this many polls (0: defaults)
     unsigned index;         // position in the call's rotation list
     int fx_unit1, fx_unit2; // fixed-point units of the bound ledger (see fixed_terms)

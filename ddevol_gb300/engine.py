@@ -236,6 +236,50 @@ class DeviceMap:
                                           C.byref(ledger), err, len(err))
         return st, ledger, err.value.decode()
 
+    def rotate_enclosed(self, rotations, opts=None, ledger=None):
+        """Validated rotations (tpgp_gb_rotate_enclosed): rotations are
+        (i, j, qi, qj, c, s, rc, rs) tuples.  Returns (status, ledger, message)."""
+        opts = opts if opts is not None else options()
+        ledger = ledger if ledger is not None else GbLedger()
+        rots = list(rotations)
+        arr = (native.GbRotation * max(1, len(rots)))()
+        for k, r in enumerate(rots):
+            arr[k] = native.GbRotation(*r)
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_rotate_enclosed(self.ptr, arr, len(rots), C.byref(opts),
+                                              C.byref(ledger), err, len(err))
+        return st, ledger, err.value.decode()
+
+    def autotune(self, terms, dt, opts=None):
+        """Times one step per candidate engine configuration from the current
+        state (which is kept) and applies the fastest (tpgp_gb_map_autotune).
+        Returns {"chosen", "before", "tried"} as dicts."""
+        opts = opts if opts is not None else options()
+        arr, count = self._terms(terms)
+        tuning = native.GbTuning()
+        err = C.create_string_buffer(512)
+        st = self.lib.tpgp_gb_map_autotune(self.ptr, arr, count, dt, C.byref(opts), C.byref(tuning),
+                                           err, len(err))
+        if st:
+            raise RuntimeError(f"autotune failed ({STATUS_NAMES[st]}): {err.value.decode()}")
+        return {"chosen": tuning.chosen.as_dict(), "before": tuning.before.as_dict(),
+                "tried": [tuning.tried[k].as_dict() for k in range(tuning.tried_count)]}
+
+    def engine_config(self):
+        c = native.GbEngineConfig()
+        if self.lib.tpgp_gb_map_get_config(self.ptr, C.byref(c)):
+            raise RuntimeError("tpgp_gb_map_get_config failed")
+        return c.as_dict()
+
+    def set_engine_config(self, **fields):
+        c = native.GbEngineConfig()
+        if self.lib.tpgp_gb_map_get_config(self.ptr, C.byref(c)):
+            raise RuntimeError("tpgp_gb_map_get_config failed")
+        for k, v in fields.items():
+            setattr(c, k, v)
+        if self.lib.tpgp_gb_map_set_config(self.ptr, C.byref(c)):
+            raise ValueError(f"invalid engine configuration {fields}")
+
     def evolve(self, terms, dt, steps, opts=None, ledger=None, record_fid=True):
         opts = opts if opts is not None else options()
         ledger = ledger if ledger is not None else GbLedger()

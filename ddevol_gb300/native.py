@@ -54,6 +54,30 @@ class GbCheckpoint(C.Structure):
                 ("stop_reason", C.c_int), ("last_status", C.c_int)]
 
 
+class GbRotation(C.Structure):
+    """tpgp_gb_rotation: one rotation with the caller's factors c, s and radii rc, rs."""
+
+    _fields_ = [("i", C.c_size_t), ("j", C.c_size_t), ("qi", C.c_uint), ("qj", C.c_uint),
+                ("c", C.c_double), ("s", C.c_double), ("rc", C.c_double), ("rs", C.c_double)]
+
+
+class GbEngineConfig(C.Structure):
+    """tpgp_gb_engine_config (include/tpgp_gb300.h): a map's step-engine launch configuration."""
+
+    _fields_ = [("hash_step", C.c_int), ("hash_ctas", C.c_int), ("hash_pdl", C.c_int),
+                ("hash_fuse", C.c_int), ("sorted_pdl", C.c_int), ("step_ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GbTuning(C.Structure):
+    """tpgp_gb_tuning: the autotuner's choice, the entry configuration and every trial."""
+
+    _fields_ = [("chosen", GbEngineConfig), ("before", GbEngineConfig), ("tried_count", C.c_size_t),
+                ("tried", GbEngineConfig * 16)]
+
+
 class GbOptions(C.Structure):
     _fields_ = [("threshold", C.c_double), ("max_terms", C.c_size_t),
                 ("max_drop_l2", C.c_double), ("exact_ledger", C.c_int), ("use_graphs", C.c_int),
@@ -129,6 +153,16 @@ def _bind(lib):
     lib.tpgp_gb_strang_step.restype = C.c_int
     lib.tpgp_gb_strang_step.argtypes = [C.c_void_p, P(GbTerm), sz, C.c_double, P(GbOptions),
                                         P(GbLedger), charp, sz]
+    lib.tpgp_gb_rotate_enclosed.restype = C.c_int
+    lib.tpgp_gb_rotate_enclosed.argtypes = [C.c_void_p, P(GbRotation), sz, P(GbOptions),
+                                            P(GbLedger), charp, sz]
+    lib.tpgp_gb_map_autotune.restype = C.c_int
+    lib.tpgp_gb_map_autotune.argtypes = [C.c_void_p, P(GbTerm), sz, C.c_double, P(GbOptions),
+                                         P(GbTuning), charp, sz]
+    lib.tpgp_gb_map_get_config.restype = C.c_int
+    lib.tpgp_gb_map_get_config.argtypes = [C.c_void_p, P(GbEngineConfig)]
+    lib.tpgp_gb_map_set_config.restype = C.c_int
+    lib.tpgp_gb_map_set_config.argtypes = [C.c_void_p, P(GbEngineConfig)]
     lib.tpgp_gb_evolve.restype = C.c_int
     lib.tpgp_gb_evolve.argtypes = [C.c_void_p, P(GbTerm), sz, C.c_double, sz, P(GbOptions),
                                    P(GbLedger), f64p, P(sz), charp, sz]

@@ -128,6 +128,70 @@ tpgp_gb_status tpgp_gb_strang_step(tpgp_gb_map *map, const tpgp_gb_term *terms, 
                                    double dt, const tpgp_gb_options *options,
                                    tpgp_gb_ledger *ledger, char *error, size_t error_capacity);
 
+/* The step engine's launch configuration for a map.  hash_step: 1 lets
+ * steps of maps up to the size crossover run as the hash-table step, 0 keeps
+ * every step on the sorted per-rotation kernels; hash_ctas: CTAs per SM of
+ * the hash pass (1-4, the pass's grid); hash_pdl / sorted_pdl: programmatic
+ * dependent launch between consecutive passes / sorted kernels; hash_fuse:
+ * consecutive rotations on one site pair in one fused pass (bound ledger).
+ * Results are bitwise the same under every configuration; only the time
+ * differs.  step_ms: a measured step time, 0 when not measured. */
+typedef struct {
+    int hash_step, hash_ctas, hash_pdl, hash_fuse, sorted_pdl;
+    double step_ms;
+} tpgp_gb_engine_config;
+
+#define TPGP_GB_TUNING_MAX 16
+typedef struct {
+    tpgp_gb_engine_config chosen;  /* applied to the map */
+    tpgp_gb_engine_config before;  /* the map's configuration on entry, timed */
+    size_t tried_count;
+    tpgp_gb_engine_config tried[TPGP_GB_TUNING_MAX];
+} tpgp_gb_tuning;
+
+tpgp_gb_status tpgp_gb_map_get_config(const tpgp_gb_map *map, tpgp_gb_engine_config *config);
+tpgp_gb_status tpgp_gb_map_set_config(tpgp_gb_map *map, const tpgp_gb_engine_config *config);
+
+/* Times one Strang step of the terms from the map's current state under
+ * each candidate configuration (the engine choice, the hash pass's CTAs per
+ * SM, dependent launch, fusion), each after one untimed step that captures
+ * its graphs, restoring the state after every trial; applies the fastest and
+ * reports all.  The map's contents are unchanged.  Device time by CUDA
+ * events, as tpgp_gb_last_elapsed_ms. */
+tpgp_gb_status tpgp_gb_map_autotune(tpgp_gb_map *map, const tpgp_gb_term *terms, size_t count,
+                                    double dt, const tpgp_gb_options *options,
+                                    tpgp_gb_tuning *tuning, char *error, size_t error_capacity);
+
+/* One rotation with the caller's trigonometric factors: c, s the cosine and
+ * sine of the angle 2*h*duration, rc, rs >= 0 bounds on their errors (the
+ * reference computes these with MPFR, engine/src/tpgp_rev.c:484-523). */
+typedef struct {
+    size_t i, j;
+    unsigned qi, qj;
+    double c, s, rc, rs;
+} tpgp_gb_rotation;
+
+/* Validated rotations (tpgp_options.validated = 1 in the reference,
+ * rotate_product at engine/src/tpgp_rev.c:535-771) with host-supplied
+ * factors and radii, in order, transactional over the list.  Keys, values
+ * and the dropped sums are those of the plain rotation; every child also
+ * carries an error radius, upadd(upmul(|v|, rc), round_radius(v c)) for the
+ * cosine child and the same with rs for the sine child (:459-464); merging
+ * adds a key's radii and, where two nonzero contributions meet, the
+ * rounding radius of their sum (:699-706); and arithmetic_l2 grows by the
+ * upper L2 of the nonzero merged radii in key order (:711-712, :734-738;
+ * the sum of upmul squares and the next double above its square root, the
+ * reference's upper_l2 without MPFR, :57-62).  A nonfinite child or merged
+ * radius is ENUMERIC; arithmetic_enclosed becomes 0 (no MPFR enclosure).
+ * The ledger is the exact one whatever options.exact_ledger says.  Runs on
+ * the hash-table step at any map size.  Rotations up to the first invalid
+ * one (site, generator, or a nonfinite or negative factor or radius) are
+ * applied and the call then returns EINVAL with the map and ledger
+ * unchanged; an empty map is a no-op. */
+tpgp_gb_status tpgp_gb_rotate_enclosed(tpgp_gb_map *map, const tpgp_gb_rotation *rotations,
+                                       size_t count, const tpgp_gb_options *options,
+                                       tpgp_gb_ledger *ledger, char *error, size_t error_capacity);
+
 /* `steps` Strang steps in a row, the reference CLI's time loop
  * (engine/src/cli_rev.c:575-670) without I/O: after each accepted step k
  * (0-based) fid_sums[k] receives tpgp_gb_single_sum(map, 1) when fid_sums

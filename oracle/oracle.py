@@ -88,6 +88,22 @@ class OptionsStruct(C.Structure):
     ]
 
 
+class RotationStruct(C.Structure):
+    """orc_rotation: one rotation with explicit factors c, s and radii rc, rs."""
+
+    _fields_ = [("i", C.c_size_t), ("j", C.c_size_t), ("qi", C.c_uint), ("qj", C.c_uint),
+                ("c", C.c_double), ("s", C.c_double), ("rc", C.c_double), ("rs", C.c_double)]
+
+
+def rotations_array(rots):
+    """rots: iterable of (i, j, qi, qj, c, s, rc, rs) -> ctypes array of RotationStruct."""
+    rots = list(rots)
+    arr = (RotationStruct * max(1, len(rots)))()
+    for k, r in enumerate(rots):
+        arr[k] = RotationStruct(*r)
+    return arr, len(rots)
+
+
 def n_words_for(n_spins: int) -> int:
     return (n_spins + 31) // 32
 
@@ -144,6 +160,9 @@ class Oracle:
             C.c_size_t, C.c_size_t, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_double,
             C.c_double, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_double),
             C.POINTER(C.c_double)]
+        lib.orc_rotations_enclosed.argtypes = [
+            C.POINTER(MapStruct), C.POINTER(RotationStruct), C.c_size_t, C.c_double, C.c_size_t,
+            C.c_double, C.POINTER(LedgerStruct)]
         lib.orc_max_threads.restype = C.c_int
         for name in ("orc_liouvillian", "orc_liouvillian_sorted"):
             getattr(lib, name).argtypes = [C.POINTER(MapStruct), C.POINTER(MapStruct),
@@ -197,6 +216,17 @@ class Oracle:
         led = ledger if ledger is not None else LedgerStruct()
         st = self.lib.orc_rotate(C.byref(m), i, j, qi, qj, h, duration, threshold, max_terms,
                                  max_drop_l2, threads, C.byref(led))
+        k, v = self._unmap(m)
+        return st, k, v, led
+
+    def rotations_enclosed(self, keys, values, n_spins, rots, threshold=0.0, max_terms=0,
+                           max_drop_l2=0.0, ledger=None):
+        """Validated rotations with explicit (c, s, rc, rs), in order, transactional."""
+        arr, count = rotations_array(rots)
+        m = self._map(keys, values, n_spins)
+        led = ledger if ledger is not None else LedgerStruct()
+        st = self.lib.orc_rotations_enclosed(C.byref(m), arr, count, threshold, max_terms,
+                                             max_drop_l2, C.byref(led))
         k, v = self._unmap(m)
         return st, k, v, led
 

@@ -362,6 +362,220 @@ out:
     return status;
 }
 
+/*
+ * One validated rotation with caller-supplied trigonometric factors c, s and
+ * their error radii rc, rs: rotate_product with validated = 1 (tpgp_rev.c:
+ * 535-771), where the reference takes c, s, rc, rs from MPFR enclosures
+ * (:484-523).  Every raw child carries a radius: 0 for a commuting key's
+ * children, upadd(upmul(|v|, rc), round_radius(v c)) and
+ * upadd(upmul(|v|, rs), round_radius(v s)) for an anticommuting key's
+ * (:459-464); a nonfinite child value or radius is ENUMERIC (:682-688).
+ * Merging adds the radii of a key's contributions with upadd, and when two
+ * nonzero contributions meet, the rounding radius of their sum (:699-706);
+ * every output key with a nonzero merged radius, kept, removed or zero,
+ * enters arithmetic_l2's upper L2 in key order (:711-712, :734-738), here
+ * the reference's non-MPFR upper_l2 (:57-62).  Keys, values and the dropped
+ * sums are those of the non-validated rotation.  An empty map is a no-op.
+ */
+int orc_rotate_enclosed(orc_map *map, size_t i, size_t j, unsigned qi, unsigned qj, double c,
+                        double s, double rc, double rs, double threshold, size_t max_terms,
+                        double max_drop_l2, orc_ledger *ledger) {
+    if (!map || !ledger || !map->n_spins || map->n_words != (map->n_spins + 31) / 32 ||
+        i >= map->n_spins || j >= map->n_spins || i == j || qi > 3 || qj > 3 || !isfinite(c) ||
+        !isfinite(s) || !isfinite(rc) || !isfinite(rs) || rc < 0 || rs < 0 ||
+        !isfinite(threshold) || threshold < 0 || !isfinite(max_drop_l2) || max_drop_l2 < 0)
+        return ORC_EINVAL;
+    if (!isfinite(ledger->dropped_l1) || ledger->dropped_l1 < 0 || !isfinite(ledger->dropped_l2) ||
+        ledger->dropped_l2 < 0 || !isfinite(ledger->dropped_l2_squared) ||
+        ledger->dropped_l2_squared < 0 || !isfinite(ledger->arithmetic_l2) ||
+        ledger->arithmetic_l2 < 0)
+        return ORC_EINVAL;
+    if (map->len == 0)
+        return ORC_OK;
+    const size_t words = map->n_words, n = map->len, slots = 2 * n;
+    uint64_t *raw_keys = malloc(slots * words * sizeof(uint64_t));
+    uint64_t *out_keys = malloc(slots * words * sizeof(uint64_t));
+    double *raw_values = malloc(slots * sizeof(double)), *out_values = malloc(slots * sizeof(double));
+    double *rad = calloc(slots, sizeof(double)), *removed = malloc(slots * sizeof(double));
+    double *merged = malloc(slots * sizeof(double));
+    size_t *idx = malloc(slots * sizeof(size_t)), *tmp = malloc(slots * sizeof(size_t));
+    int status = ORC_OK;
+    if (!raw_keys || !out_keys || !raw_values || !out_values || !rad || !removed || !merged ||
+        !idx || !tmp) {
+        status = ORC_ENOMEM;
+        goto out;
+    }
+    for (size_t k = 0; k < n; k++) {
+        const uint64_t *key = map->keys + k * words;
+        uint64_t *first = raw_keys + 2 * k * words, *second = first + words;
+        memcpy(first, key, words * sizeof(uint64_t));
+        memcpy(second, key, words * sizeof(uint64_t));
+        double v = map->values[k];
+        unsigned pi = site_symbol(key, i), pj = site_symbol(key, j);
+        if (!(anticommutes(qi, pi) ^ anticommutes(qj, pj))) {
+            raw_values[2 * k] = v;
+            raw_values[2 * k + 1] = 0;
+            continue;
+        }
+        unsigned phase = (phase_of(qi, pi) + phase_of(qj, pj)) & 3u;
+        second[i / 32] ^= (uint64_t)qi << (2 * (i % 32));
+        second[j / 32] ^= (uint64_t)qj << (2 * (j % 32));
+        double x = v * c, y = v * s;
+        raw_values[2 * k] = x;
+        raw_values[2 * k + 1] = (phase == 1 ? 1.0 : -1.0) * y;
+        rad[2 * k] = up_add(up_mul(fabs(v), rc), rounding_radius(x));
+        rad[2 * k + 1] = up_add(up_mul(fabs(v), rs), rounding_radius(y));
+    }
+    for (size_t k = 0; k < slots; k++) {
+        if (!isfinite(raw_values[k]) || !isfinite(rad[k])) {
+            status = ORC_ENUMERIC;
+            goto out;
+        }
+        idx[k] = k;
+    }
+    {  /* stable bottom-up merge sort of slot indices by key (as orc_rotate) */
+        size_t *a = idx, *b = tmp;
+        for (size_t width = 1; width < slots; width *= 2) {
+            for (size_t lo = 0; lo < slots; lo += 2 * width) {
+                size_t mid = lo + width < slots ? lo + width : slots;
+                size_t hi = lo + 2 * width < slots ? lo + 2 * width : slots;
+                size_t x = lo, y = mid, o = lo;
+                while (x < mid && y < hi) {
+                    if (key_order(raw_keys + a[x] * words, raw_keys + a[y] * words, words) <= 0)
+                        b[o++] = a[x++];
+                    else
+                        b[o++] = a[y++];
+                }
+                while (x < mid)
+                    b[o++] = a[x++];
+                while (y < hi)
+                    b[o++] = a[y++];
+            }
+            size_t *t = a;
+            a = b;
+            b = t;
+        }
+        if (a != idx)
+            memcpy(idx, a, slots * sizeof(size_t));
+    }
+    size_t out_len = 0, discarded = 0, nrad = 0;
+    double l1 = 0, sq = 0;
+    for (size_t k = 0; k < slots;) {
+        size_t p = idx[k++];
+        const uint64_t *key = raw_keys + p * words;
+        double v = raw_values[p], r = rad[p];
+        while (k < slots && key_order(key, raw_keys + idx[k] * words, words) == 0) {
+            size_t q = idx[k++];
+            double previous = v;
+            v += raw_values[q];
+            r = up_add(r, rad[q]);
+            if (previous != 0 && raw_values[q] != 0)
+                r = up_add(r, rounding_radius(v));
+        }
+        if (!isfinite(v) || !isfinite(r)) {
+            status = ORC_ENUMERIC;
+            goto out;
+        }
+        if (r != 0)
+            merged[nrad++] = r;
+        if (v == 0)
+            continue;
+        int identity = 1;
+        for (size_t w = 0; w < words; w++)
+            identity &= key[w] == 0;
+        if (!identity && fabs(v) <= threshold) {
+            removed[discarded++] = fabs(v);
+            l1 = up_add(l1, fabs(v));
+            sq = up_add(sq, up_mul(v, v));
+            continue;
+        }
+        memcpy(out_keys + out_len * words, key, words * sizeof(uint64_t));
+        out_values[out_len++] = v;
+    }
+    if (max_terms && out_len > max_terms) {
+        status = ORC_ECAP;
+        goto out;
+    }
+    {
+        double sum = 0, rsum = 0;
+        for (size_t k = 0; k < discarded; k++)
+            sum = up_add(sum, up_mul(removed[k], removed[k]));
+        for (size_t k = 0; k < nrad; k++)
+            rsum = up_add(rsum, up_mul(merged[k], merged[k]));
+        double l2 = sum == 0 ? 0 : nextafter(sqrt(sum), INFINITY);
+        double ar = rsum == 0 ? 0 : nextafter(sqrt(rsum), INFINITY);
+        orc_ledger next = *ledger;
+        next.dropped_l1 = up_add(next.dropped_l1, l1);
+        next.dropped_l2 = up_add(next.dropped_l2, l2);
+        next.dropped_l2_squared = up_add(next.dropped_l2_squared, sq);
+        next.arithmetic_l2 = up_add(next.arithmetic_l2, ar);
+        next.rotations++;
+        if (discarded)
+            next.removal_events++;
+        if (out_len > next.peak_terms)
+            next.peak_terms = out_len;
+        next.arithmetic_enclosed = 0;  /* no MPFR: tpgp_rev.c:744 */
+        if (!isfinite(next.dropped_l2) || !isfinite(next.arithmetic_l2)) {
+            status = ORC_ENUMERIC;
+            goto out;
+        }
+        if (max_drop_l2 && next.dropped_l2 > max_drop_l2) {
+            status = ORC_EBUDGET;
+            goto out;
+        }
+        free(map->keys);
+        free(map->values);
+        map->keys = out_keys;
+        map->values = out_values;
+        map->len = out_len;
+        map->capacity = slots;
+        out_keys = NULL;
+        out_values = NULL;
+        *ledger = next;
+    }
+out:
+    free(raw_keys);
+    free(out_keys);
+    free(raw_values);
+    free(out_values);
+    free(rad);
+    free(removed);
+    free(merged);
+    free(idx);
+    free(tmp);
+    return status;
+}
+
+/* A list of validated rotations applied in order, transactional over the
+ * list (the map and ledger change only when every rotation succeeds). */
+typedef struct {
+    size_t i, j;
+    unsigned qi, qj;
+    double c, s, rc, rs;
+} orc_rotation;
+int orc_rotations_enclosed(orc_map *map, const orc_rotation *rots, size_t count, double threshold,
+                           size_t max_terms, double max_drop_l2, orc_ledger *ledger) {
+    if (!map || (!rots && count) || !ledger)
+        return ORC_EINVAL;
+    orc_map work;
+    int status = orc_map_from_arrays(&work, map->n_spins, map->keys, map->values, map->len);
+    if (status)
+        return status;
+    orc_ledger next = *ledger;
+    for (size_t k = 0; k < count && !status; k++)
+        status = orc_rotate_enclosed(&work, rots[k].i, rots[k].j, rots[k].qi, rots[k].qj,
+                                     rots[k].c, rots[k].s, rots[k].rc, rots[k].rs, threshold,
+                                     max_terms, max_drop_l2, &next);
+    if (status) {
+        orc_map_free(&work);
+        return status;
+    }
+    orc_map_free(map);
+    *map = work;
+    *ledger = next;
+    return ORC_OK;
+}
+
 static int map_copy(orc_map *dst, const orc_map *src) {
     return orc_map_from_arrays(dst, src->n_spins, src->keys, src->values, src->len);
 }

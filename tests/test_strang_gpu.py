@@ -147,6 +147,25 @@ def test_transactional_cap_and_budget(engine, golden_trajectories, exact):
     m.close()
 
 
+def test_invalid_term_after_buffer_allocation(engine, golden_trajectories):
+    """A step on a map that has already stepped (its current buffer is not
+    the first) which allocates device buffers (the exact ledger's log, a
+    longer parameter list) and then reaches an invalid term restores the
+    committed map, not the arena's first buffer."""
+    g = golden_trajectories
+    p, terms = load_traj(g, "ring16")
+    m = engine.map(16, g[p + "in_keys"], g[p + "in_values"])
+    st, led, msg = m.strang_step(terms, 0.01, options(1e-6, exact_ledger=False), GbLedger())
+    assert st == 0, msg
+    k0, v0 = m.download()
+    bad = list(terms[:5]) + [(3, 3, 1, 1, 0.1)]
+    st, _, _ = m.strang_step(bad, 0.01, options(1e-6, exact_ledger=True), GbLedger())
+    assert st == 1
+    k, v = m.download()
+    m.close()
+    assert np.array_equal(k, k0) and np.array_equal(bits(v), bits(v0))
+
+
 @pytest.mark.parametrize("exact", [True, False])
 def test_growth_across_arena_resize(engine, oracle, exact):
     """Start from a tiny arena and grow through several reallocations in one call."""
