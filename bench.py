@@ -13,6 +13,9 @@ exactly K steps are timed.
 
 Metric: Pauli terms/s = (sum over the timed rotations of the rotation's input
 terms) / device time of the K steps (CUDA events on the engine's stream).
+The timed steps use the ABI's default exact ledger, so every output of the
+timed path (keys, values, FIDs, ledger) is bitwise the reference's;
+--bound-ledger times the fixed-point ledger instead.
 
 Extra keys: e2e (the same K steps from the same state through the C-ABI
 with pinned host buffers, L2 flushed before each step as in the device leg:
@@ -22,7 +25,7 @@ launch over its mean launch time, from CUDA events captured into the timed
 steps' graphs), cpu_baseline (the CPU implementation on rotations spread
 over one whole step of the window state), clocks (nvidia-smi sampled during
 the timed region), gpu_launches, and forms: the plain single solve (16-spin
-ring, 400 steps), one step with the exact ledger, the batched powder
+ring, 400 steps), one step with the other ledger, the batched powder
 average and the serving stream, each bounded in time, with FID solves/s,
 roofline fraction and clocks.
 
@@ -359,7 +362,8 @@ def run_gb300(args, dist):
     words = (cfg["n"] + 31) // 32
     terms = cfg["terms"]()
     eng = Engine(dist.local_rank)
-    opts = options(cfg["threshold"], exact_ledger=args.exact_ledger, use_graphs=True)
+    exact = not args.bound_ledger
+    opts = options(cfg["threshold"], exact_ledger=exact, use_graphs=True)
     win = window_state(args.config) if not args.setup else None
     if win is not None:
         k_win, v_win, step0 = win
@@ -374,9 +378,10 @@ def run_gb300(args, dist):
     # the engine's launch configuration for this workload: one timed step per
     # candidate from the start state (kept), the fastest applied (before the
     # warm-up; the e2e leg steps the same map)
-    tuning = None
+    tuning, tuned = None, None
     if not args.no_autotune:
         t = m.autotune(terms, cfg["dt"], opts)
+        tuned = t["chosen"]
         name = lambda c: (f"hash ctas={c['hash_ctas']} pdl={c['hash_pdl']} fuse={c['hash_fuse']}"
                           if c["hash_step"] else f"sorted pdl={c['sorted_pdl']}")
         tuning = {"chosen": name(t["chosen"]), "chosen_ms": round(t["chosen"]["step_ms"], 3),
@@ -387,7 +392,7 @@ def run_gb300(args, dist):
     # With the hash-table step the per-phase CUDA events are part of each
     # step's graph, so the dominant kernel's launch time is measured on the
     # timed steps themselves; the warm-up steps capture that same graph.
-    live_profile = not args.exact_ledger
+    live_profile = m.engine_config()["hash_step"] == 1
     m.set_profiling(live_profile)
     for _ in range(args.warmup):
         st, _, led, msg = m.evolve(terms, cfg["dt"], 1, opts, led)
@@ -523,7 +528,7 @@ def run_gb300(args, dist):
                              f"rotation calls), each applied to the {len(v_win)}-term window "
                              f"state"}
         if not args.no_forms:
-            forms = run_forms(args, eng, k_win, v_win, terms, cfg, peak)
+            forms = run_forms(args, eng, k_win, v_win, terms, cfg, peak, tuned)
     m.close()
     eng.close()
     line = {
@@ -534,7 +539,8 @@ def run_gb300(args, dist):
         "config": workload_config(args, cfg, terms, words, start),
         "window": {"timed_steps_after_state": [args.warmup, args.warmup + args.steps],
                    "terms_at_timed_start": n_before, "terms_after": n_after,
-                   "ledger": "exact (sequential)" if args.exact_ledger else "bound (fixed-point)",
+                   "ledger": "exact (sequential, bitwise the reference's)" if exact
+                             else "bound (fixed-point)",
                    "l2": f"map {n_before * (8 * words + 8) / 1e6:.1f} MB per buffer; L2 flushed "
                          f"(512 MB write) between timed steps"},
         "e2e": e2e,
@@ -602,6 +608,7 @@ def plain_solve(eng, peak, budget_s=None, warm=True):
     path_bytes = algorithmic_bytes(1, r["terms"], r["terms"])
     complete = r["steps"] >= steps
     out = {"workload": "ring16 J1=1 J2=1/8, X_0, dt=0.01, 400 steps, threshold 1e-6",
+           "ledger": "bound (fixed-point)",
            "steps_reached": r["steps"], "steps_total": steps, "complete": complete,
            "value": r["terms"] / r["wall"], "unit": METRIC,
            "device_value": r["terms"] / (r["dev_ms"] / 1e3),
@@ -640,13 +647,17 @@ def run_plain_solve(args, dist):
             "plain_solve": r, "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}
 
 
-def form_exact_ledger(eng, k_win, v_win, terms, cfg, peak):
-    """One Strang step of the window with the exact (sequential, bitwise
-    reference) ledger, the ABI's default, after two untimed steps from the
-    same state (graph capture, log and table sizing)."""
+def form_ledger(eng, k_win, v_win, terms, cfg, peak, exact, tuned):
+    """One Strang step of the window with the given ledger (exact: the
+    sequential, bitwise-reference sums, the ABI's default; else the
+    fixed-point bound), under the headline's tuned engine configuration,
+    after two untimed steps from the same state (graph capture, log and
+    table sizing)."""
     from ddevol_gb300.engine import GbLedger, options
-    opts = options(cfg["threshold"], exact_ledger=True)
+    opts = options(cfg["threshold"], exact_ledger=exact)
     m = eng.map(cfg["n"], k_win, v_win)
+    if tuned:
+        m.set_engine_config(**{k: v for k, v in tuned.items() if k != "step_ms"})
     for _ in range(2):
         st, _, _, msg = m.evolve(terms, cfg["dt"], 1, opts, GbLedger())
         if st:
@@ -661,18 +672,21 @@ def form_exact_ledger(eng, k_win, v_win, terms, cfg, peak):
     ms = m.last_elapsed_ms()
     m.close()
     b = algorithmic_bytes(words, t, t + n1 - len(v_win))
-    return {"workload": "the ring64 window, one Strang step, exact ledger", "value": t / (ms / 1e3),
+    return {"workload": "the ring64 window, one Strang step, "
+                        + ("exact ledger" if exact else "bound ledger"), "value": t / (ms / 1e3),
             "unit": METRIC, "ms_per_step": ms,
             "roofline": {"bound": "hbm", "frac": b / (ms / 1e3) / 1e9 / peak, "peak": peak,
                          "basis": "whole step over device time"}}
 
 
-def run_forms(args, eng, k_win, v_win, terms, cfg, peak):
+def run_forms(args, eng, k_win, v_win, terms, cfg, peak, tuned=None):
     """Bounded sub-lines of the other forms, and one step of the window with
-    the ABI's default exact ledger."""
+    the other ledger than the headline's."""
     forms = {}
+    other = "bound_ledger" if not args.bound_ledger else "exact_ledger"
     todo = [("plain_solve", lambda: plain_solve(eng, peak, budget_s=args.form_seconds)),
-            ("exact_ledger", lambda: form_exact_ledger(eng, k_win, v_win, terms, cfg, peak)),
+            (other, lambda: form_ledger(eng, k_win, v_win, terms, cfg, peak, args.bound_ledger,
+                                        tuned)),
             ("powder", lambda: powder_form(args, eng, peak)),
             ("serve", lambda: serve_form(args, eng, peak))]
     for name, fn in todo:
@@ -736,7 +750,8 @@ def powder_summary(r, peak):
     complete = r["reached"] >= POWDER["steps_total"]
     per_step_s = r["ms"] / 1e3 / max(1, r["steps"])
     b = algorithmic_bytes(1.5, r["terms"], r["terms"])  # W = 1 or 2 per item: 40 B per term
-    out = {"workload": "powder_batch", "items": r["items"], "value": r["terms"] / (r["ms"] / 1e3),
+    out = {"workload": "powder_batch", "ledger": "bound (fixed-point)", "items": r["items"],
+           "value": r["terms"] / (r["ms"] / 1e3),
            "unit": METRIC, "steps_timed": r["steps"], "steps_reached": r["reached"],
            "steps_total": POWDER["steps_total"], "complete": complete,
            "ms_per_batched_step": per_step_s * 1e3,
@@ -852,7 +867,8 @@ def serve_run(eng, seed, seconds):
 def serve_summary(r, peak):
     st = r["st"]
     b = algorithmic_bytes(2, st["terms"], st["terms"])  # key widths 1-3 words: 48 B per term
-    return {"workload": "serve_stream", "requests": r["count"], "rate_per_s": r["rate"],
+    return {"workload": "serve_stream", "ledger": "bound (fixed-point)", "requests": r["count"],
+            "rate_per_s": r["rate"],
             "value": st["terms"] / st["wall_seconds"], "unit": METRIC,
             "fid_solves_per_s": (r["count"] - r["failed"]) / st["wall_seconds"],
             "latency_s_p50": float(np.percentile(r["lat"], 50)),
@@ -986,11 +1002,12 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the engine's default launch configuration (no tpgp_gb_map_autotune)")
     ap.add_argument("--no-forms", action="store_true",
-                    help="skip the plain-solve, exact-ledger, powder and serving sub-lines")
+                    help="skip the plain-solve, other-ledger, powder and serving sub-lines")
     ap.add_argument("--form-seconds", type=float, default=15.0,
                     help="wall budget of the plain-solve, powder and serving sub-lines")
-    ap.add_argument("--exact-ledger", action="store_true",
-                    help="bitwise reference ledger (one sequential sum per rotation)")
+    ap.add_argument("--bound-ledger", action="store_true",
+                    help="time the fixed-point (bound) ledger instead of the ABI's default exact "
+                         "ledger (bitwise the reference's sequential sums)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

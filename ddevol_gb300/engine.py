@@ -318,7 +318,7 @@ class DeviceMap:
         return self.lib.tpgp_gb_last_terms(self.ptr)
 
     KERNELS = ("k_classify", "k_flip_sort", "k_partition", "k_merge", "k_hash_rotate",
-               "k_hash_build", "k_hash_chain_extract", "k_radix_sort")
+               "k_hash_build", "k_hash_chain_extract", "k_radix_sort", "k_hash_exact_ledger")
 
     def set_profiling(self, on=True):
         self.lib.tpgp_gb_set_profiling(self.ptr, int(bool(on)))

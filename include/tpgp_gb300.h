@@ -306,8 +306,9 @@ size_t tpgp_gb_last_terms(const tpgp_gb_map *map);
  * device milliseconds and launch counts since profiling was switched on:
  * sorted path 0 classify, 1 flip-sort, 2 partition, 3 merge (each kernel
  * bracketed); hash-table path 4 rotations, 5 table build, 6 commit chain and
- * extraction, 7 radix sort (bracketed as groups). */
-#define TPGP_GB_PROFILE_SLOTS 8
+ * extraction, 7 radix sort, 8 stat reduction and the exact ledger's segment
+ * sort and sums (bracketed as groups). */
+#define TPGP_GB_PROFILE_SLOTS 9
 void tpgp_gb_set_profiling(tpgp_gb_map *map, int on);
 void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t *launches);
 

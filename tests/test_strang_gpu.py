@@ -117,6 +117,38 @@ def test_longer_ring16_vs_oracle(engine, ring16_60_oracle, exact):
         assert led.removal_events == oled.removal_events
 
 
+@pytest.fixture(scope="module")
+def cubic30_oracle(oracle):
+    terms = H.cubic_111(4)
+    k0, v0 = H.single_site_operator(64)
+    fids_o = []
+    ost, ok, ov, oled = oracle.strang_step(k0, v0, 64, terms, 0.005, threshold=1e-5, steps=30,
+                                           threads=16, on_step=lambda s, f, n: fids_o.append(f))
+    assert ost == 0
+    return terms, k0, v0, ok, ov, oled, np.array(fids_o)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_cubic_30_steps_vs_oracle(engine, cubic30_oracle, exact):
+    """30 steps of the 4x4x4 cubic lattice (64 spins, two-word keys, 3840
+    rotations per step) from X on site 0: keys, values and every step's FID
+    bitwise; the exact ledger bitwise (through the hash-table step's
+    per-rotation segment sums), the bound ledger within its bound."""
+    terms, k0, v0, ok, ov, oled, fids_o = cubic30_oracle
+    m = engine.map(64, k0, v0)
+    st, fids, led, msg = m.evolve(terms, 0.005, 30, options(1e-5, exact_ledger=exact))
+    assert st == 0, msg
+    k, v = m.download()
+    m.close()
+    assert np.array_equal(k, ok) and np.array_equal(bits(v), bits(ov))
+    assert np.array_equal(bits(fids), bits(fids_o))
+    if exact:
+        assert np.array_equal(bits(ledger_vec(led)), bits(ledger_vec(oled)))
+    else:
+        assert abs(led.dropped_l2 - oled.dropped_l2) <= 1e-11 * oled.dropped_l2
+        assert led.removal_events == oled.removal_events
+
+
 @pytest.mark.parametrize("exact", [True, False])
 def test_transactional_cap_and_budget(engine, golden_trajectories, exact):
     g = golden_trajectories
