@@ -53,6 +53,25 @@ def test_exact_ledger_hash_matches_sorted(n_spins):
 
 
 @pytest.mark.parametrize("n_spins", [24, 60, 90, 120])
+def test_exact_ledger_multi_tile_segments(n_spins):
+    """Maps of 4·10^4 terms with values spread over six decades and a high
+    threshold, so a rotation removes thousands of terms: the per-rotation
+    segment sort runs its multi-tile passes at every key width (W = 1..4).
+    Hash-table step against the sorted kernels, everything bitwise."""
+    rng = np.random.default_rng(500 + n_spins)
+    keys, vals = random_map(rng, n_spins, 40000)
+    terms = H.ring_j1j2(n_spins, 1.0, 0.3)[:6]
+    opts = options(3e-3, exact_ledger=True)
+    a = evolve(True, n_spins, keys, vals, terms, 0.2, 1, opts)
+    b = evolve(False, n_spins, keys, vals, terms, 0.2, 1, opts)
+    assert a[0] == b[0] == 0, (a[5], b[5])
+    assert a[4].removal_events > 0 and len(a[2]) < len(vals)
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(bits(a[2]), bits(b[2]))
+    assert np.array_equal(bits(ledger_vec(a[4])), bits(ledger_vec(b[4])))
+
+
+@pytest.mark.parametrize("n_spins", [24, 60, 90, 120])
 def test_hash_matches_sorted_random_maps(n_spins):
     """Random multi-site maps (W = 1..4) under three steps of a ring with
     next-nearest couplings: hash and sorted paths bitwise equal."""
