@@ -681,6 +681,55 @@ def form_ledger(eng, k_win, v_win, terms, cfg, peak, exact, tuned):
                          "basis": "whole step over device time"}}
 
 
+def form_branch_abi(reps=10):
+    """The reference-facing CUDA branch ABI (tpgp_cuda_branches, the
+    reference's branch-backend interface) on 10^6 two-word terms from host
+    memory: copies in, branch kernel, copies out, per call, timed on the
+    host; beside it the branch loop of the CPU implementation (one thread)
+    on the same input, and the bytes the call moves over the host link."""
+    import ctypes as C
+
+    from ddevol_gb300.engine import CudaBranchContext, _f64p, _u64p
+    n, count, words = 64, 1_000_000, 2
+    rng = np.random.default_rng(11)
+    keys = rng.integers(0, 2 ** 63, size=count * words, dtype=np.int64).astype(np.uint64)
+    vals = rng.standard_normal(count)
+    i, j, qi, qj = 3, 40, 1, 1
+    c, s = math.cos(0.01), math.sin(0.01)
+    ok = np.zeros(2 * count * words, np.uint64)
+    ov = np.zeros(2 * count, np.float64)
+    orad = np.zeros(2 * count, np.float64)
+    err = C.create_string_buffer(256)
+    ctx = CudaBranchContext(0)
+    try:
+        def call():
+            st = ctx.lib.tpgp_cuda_branches(ctx.ptr, _u64p(keys), _f64p(vals), count, words, n, i, j,
+                                            qi, qj, c, s, 0.0, 0.0, 0, _u64p(ok), _f64p(ov),
+                                            _f64p(orad), err, len(err))
+            if st:
+                raise RuntimeError(err.value.decode())
+        for _ in range(2):
+            call()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        dt = (time.perf_counter() - t0) / reps
+    finally:
+        ctx.close()
+    from oracle.oracle import Oracle, build_oracle
+    build_oracle()
+    impl, kind = Oracle(), "port"
+    t0 = time.perf_counter()
+    st, _, _, _ = impl.branches(keys, vals, n, i, j, qi, qj, c, s)
+    cpu_dt = time.perf_counter() - t0
+    moved = count * (8 * words + 8) + 2 * count * (8 * words + 8 + 8)  # in; keys, values, radii out
+    return {"workload": "tpgp_cuda_branches, 10^6 terms, 128-bit keys, host arrays in and out",
+            "value": count / dt, "unit": METRIC, "ms_per_call": dt * 1e3,
+            "host_link_gbs": moved / dt / 1e9, "bytes_per_call": moved,
+            "cpu_branch": {"value": count / cpu_dt, "unit": METRIC, "cores": 1, "kind": kind,
+                           "status": st}}
+
+
 def run_forms(args, eng, k_win, v_win, terms, cfg, peak, tuned=None):
     """Bounded sub-lines of the other forms, and one step of the window with
     the other ledger than the headline's."""
@@ -690,7 +739,8 @@ def run_forms(args, eng, k_win, v_win, terms, cfg, peak, tuned=None):
             (other, lambda: form_ledger(eng, k_win, v_win, terms, cfg, peak, not args.exact_ledger,
                                         tuned)),
             ("powder", lambda: powder_form(args, eng, peak)),
-            ("serve", lambda: serve_form(args, eng, peak))]
+            ("serve", lambda: serve_form(args, eng, peak)),
+            ("branch_abi", lambda: form_branch_abi())]
     for name, fn in todo:
         try:
             forms[name] = fn()
