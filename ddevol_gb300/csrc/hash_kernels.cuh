@@ -44,7 +44,6 @@
 // step's input map is never written (transactional).
 #pragma once
 #include <cooperative_groups.h>
-#include <cooperative_groups/scan.h>
 
 #include "onesweep.cuh"
 #include "rotate_kernels.cuh"
@@ -166,32 +165,6 @@ __device__ __forceinline__ void log_entry(const HashArgs& a, const Key<W>& key,
 template <int W>
 __device__ __forceinline__ void log_removed(const HashArgs& a, const Key<W>& key, double x) {
     log_entry<W>(a, key, abs_bits(x));
-}
-// A pair's entries (K's and/or P's) with one position claim for both: the
-// threads that log together scan their counts and take one range.  Called
-// only by threads with at least one entry.
-template <int W>
-__device__ __forceinline__ void log_pair(const HashArgs& a, const Key<W>& K, unsigned long long kb,
-                                         bool has_k, const Key<W>& P, unsigned long long pb,
-                                         bool has_p) {
-    const cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
-    const unsigned cnt = (has_k ? 1u : 0u) + (has_p ? 1u : 0u);
-    const unsigned excl = cooperative_groups::exclusive_scan(g, cnt);
-    const unsigned total = g.shfl(excl + cnt, g.size() - 1);
-    unsigned long long pos = 0;
-    if (g.thread_rank() == 0) pos = atomicAdd(a.xlog_count, (unsigned long long)total);
-    pos = g.shfl(pos, 0) + excl;
-    if (has_k) {
-        if (pos < a.xlog_cap) {
-            store_key<W>(a.xlog_keys, pos, K);
-            a.xlog_vals[pos] = kb;
-        }
-        ++pos;
-    }
-    if (has_p && pos < a.xlog_cap) {
-        store_key<W>(a.xlog_keys, pos, P);
-        a.xlog_vals[pos] = pb;
-    }
 }
 
 
@@ -634,9 +607,14 @@ __device__ __forceinline__ void pair_radii(const HashArgs& a, const PassParams& 
     if (!is_finite(kc) || !is_finite(ks) || !is_finite(pc) || !is_finite(ps) || !is_finite(rk) ||
         !is_finite(rp))
         t.flags |= ST_NUMERIC;
-    const bool has_k = !is_zero(rk), has_p = !is_zero(rp);
-    t.radii += (has_k ? 1u : 0u) + (has_p ? 1u : 0u);
-    if (has_k || has_p) log_pair<W>(a, K, dbits(rk) | kSignBit, has_k, P, dbits(rp) | kSignBit, has_p);
+    if (!is_zero(rk)) {
+        log_entry<W>(a, K, dbits(rk) | kSignBit);
+        ++t.radii;
+    }
+    if (!is_zero(rp)) {
+        log_entry<W>(a, P, dbits(rp) | kSignBit);
+        ++t.radii;
+    }
 }
 
 // Index 4 pi + pj of a key's two site symbols in the pass's branch tables.
@@ -775,8 +753,8 @@ __device__ __forceinline__ void hash_pass(const HashArgs& a, const PassParams& p
                     if constexpr (V)
                         pair_radii<W>(a, p, K, P, k_live, p_live, from_bits(R.val), from_bits(pb), nk, np, t);
                     if (a.xlog_keys) {
-                        const bool lk = !kbits && !is_zero(nk), lp = !pbits && !is_zero(np);
-                        if (lk || lp) log_pair<W>(a, K, abs_bits(nk), lk, P, abs_bits(np), lp);
+                        if (!kbits && !is_zero(nk)) log_removed<W>(a, K, nk);
+                        if (!pbits && !is_zero(np)) log_removed<W>(a, P, np);
                     }
                     if (kbits != R.val) store_val<W>(a.rec, slot, kbits);
                     if (found >= 0) {
