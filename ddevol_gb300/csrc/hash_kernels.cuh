@@ -841,6 +841,22 @@ __device__ __forceinline__ void coset_sign(const RotParams& p, const Key<W>& m, 
     branch_info(p, word_at<W>(m, p.i_word), word_at<W>(m, p.j_word), anti, plus);
 }
 
+// Whether a key anticommutes with some generator of the run.  A key that
+// commutes with all of them keeps its value through the run (no flipped
+// child lands on a commuting key), so only the threshold can change it;
+// and a member of a coset that does anticommute has every pairing partner
+// anticommuting too, so the run's pairings stay among such members.
+template <int W>
+__device__ __forceinline__ bool run_participates(const HashArgs& a, unsigned r0, unsigned L,
+                                                 const Key<W>& key) {
+    for (unsigned l = 0; l < L; ++l) {
+        bool anti, plus;
+        coset_sign<W>(a.ps[r0 + l], key, anti, plus);
+        if (anti) return true;
+    }
+    return false;
+}
+
 template <int W>
 __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned k) {
     __shared__ unsigned long long s_acc[kMaxRun][4];
@@ -869,6 +885,8 @@ __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned
     }
     G[3] = key_xor<W>(G[1], G[2]);
     const int gs = has_b2 ? 4 : 2;
+    // after the step's first pass every value has passed the threshold once
+    const bool settled = k > 0 && a.ps[r0 - 1].threshold_bits == a.ps[r0].threshold_bits;
     unsigned flags = 0u;
     const unsigned long long S = a.slots;
     const unsigned long long len = min(__ldcg(a.claimed), S);
@@ -888,9 +906,29 @@ __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned
         const uint32_t slot = E.slot;
         Rec<W> R;
         R.tag = stamp;
-        if (slot != kNoSlot && E.stamp < stamp) R = load_rec<W>(a.rec, slot);
-        if (R.tag < stamp) {
+        bool part = false;
+        if (slot != kNoSlot && E.stamp < stamp) {
+            part = run_participates<W>(a, r0, L, E.key);
+            if (part || !settled) R = load_rec<W>(a.rec, slot);
+        }
+        if (R.tag < stamp && !part) {
+            // commutes with the whole run: the run's first rotation thresholds
+            // the unchanged value, the later ones see the same value
+            if (R.val) {
+                PairTally t = empty_tally();
+                const unsigned long long out = settle<W>(a.ps[r0], R.key, from_bits(R.val), true, t);
+                if (out != R.val) store_val<W>(a.rec, slot, out);
+                if (t.removed) {
+                    shared_add_u128(s_acc[0], t.l1);
+                    shared_add_u128(s_acc[0] + 2, t.sq);
+                    atomicAdd(&s_cnt[0][2], t.removed);
+                }
+                if (t.died) atomicAdd(&s_cnt[0][1], t.died);
+                flags |= t.flags;
+            }
+        } else if (R.tag < stamp) {
             // the coset's other members: first probe records loaded together
+            // (only those that take part in the run; the others keep to themselves)
             Key<W> M[4];
             Rec<W> PR[4];
             unsigned long long ps[4], ea[4], v[4];
@@ -899,13 +937,16 @@ __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned
             sl[0] = (long long)slot;
             v[0] = R.val;
             ea[0] = 0ull;
+            bool mp[4];
+            mp[0] = true;
 #pragma unroll
             for (int m = 1; m < 4; ++m) {
                 M[m] = key_xor<W>(R.key, G[m]);
                 sl[m] = -1;
                 v[m] = 0ull;
                 ea[m] = 0ull;
-                if (m < gs) {
+                mp[m] = m < gs && run_participates<W>(a, r0, L, M[m]);
+                if (mp[m]) {
                     ps[m] = slot_of(hash_of<W>(M[m]), S);
                     PR[m] = load_rec<W>(a.rec, ps[m]);
                 }
@@ -913,7 +954,7 @@ __global__ void __launch_bounds__(kHashBlock, 2) k_hash_run(HashArgs a, unsigned
             bool overflow = false;
 #pragma unroll
             for (int m = 1; m < 4; ++m) {
-                if (m >= gs) continue;
+                if (!mp[m]) continue;  // absent from the run's pairings: never probed, never written
                 sl[m] = probe_from<W>(a, M[m], ps[m], PR[m], stamp, &ea[m], &v[m], &overflow);
             }
             // owner: the smallest present member; a coset with no live member has nothing to do
