@@ -81,7 +81,7 @@ typedef struct {
 typedef struct tpgp_gb_context tpgp_gb_context;
 typedef struct tpgp_gb_map tpgp_gb_map;
 
-/* Library and device.  compiled() is 1 for this build.  create() binds one
+/* Library and device.  compiled() returns 1 (the library has its device code).  create() binds one
  * device (index as CUDA_VISIBLE_DEVICES numbers it) and a stream; NULL with
  * a message when the device is missing.  Replaces the context part of
  * engine/include/tpgp_cuda_rev.h:20-23 for the device-resident path. */

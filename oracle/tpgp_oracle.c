@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY. This file restates, in plain C, the reference
  * engine's CPU algorithm for one secular two-spin rotation of a sparse Pauli
- * map (DDevol engine/src/tpgp_rev.c).  It is the parity checker for the CUDA
+ * map (DDevol engine/src/tpgp_rev.c).  It is the parity oracle for the CUDA
  * path and the CPU baseline timed by bench.py; no product code path links or
  * calls it.  Only tests/, __graft_entry__.smoke() and bench.py load it.
  *

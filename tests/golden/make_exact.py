@@ -1,4 +1,4 @@
-"""Generate the fixtures that pin the exact-FID and Strang-bound checkers.
+"""Generate the fixtures that pin the exact-FID and Strang-bound references.
 
 Writes ``exact.npz`` next to this script:
 

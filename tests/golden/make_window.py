@@ -16,7 +16,7 @@ Files written next to this script:
   (DDevol engine/src/tpgp_rev.c, built by ``make -C oracle ref``) from that
   state: output keys, values, ledger (from a zero ledger), FID sum.
 
-    python tests/golden/make_window.py --state      # on a GPU machine
+    python tests/golden/make_window.py --state      # on a machine with a GB300
     DDEVOL_REFERENCE=<checkout> make -C oracle ref
     python tests/golden/make_window.py --expect     # a few minutes on the CPU
 """
