@@ -29,27 +29,7 @@
 #include <omp.h>
 #endif
 
-/* Status codes follow tpgp_status (engine/include/tpgp_rev.h:9-17). */
-enum { ORC_OK = 0, ORC_EINVAL, ORC_ENOMEM, ORC_ECAP, ORC_ENUMERIC, ORC_EBACKEND, ORC_EBUDGET };
-
-/* Same field order as tpgp_map / tpgp_ledger / tpgp_term (tpgp_rev.h:25-51). */
-typedef struct {
-    size_t n_spins, n_words, len, capacity;
-    uint64_t *keys;
-    double *values;
-} orc_map;
-typedef struct {
-    size_t i, j;
-    unsigned qi, qj;
-    double h;
-    size_t layer;
-} orc_term;
-typedef struct {
-    double dropped_l1, dropped_l2, dropped_l2_squared;
-    double arithmetic_l2;
-    size_t rotations, removal_events, peak_terms;
-    int arithmetic_enclosed;
-} orc_ledger;
+#include "tpgp_oracle.h"
 
 /* Directed-rounding helpers: tpgp_rev.c:25-42. */
 static double up_add(double a, double b) {
@@ -177,6 +157,15 @@ int orc_branches(const uint64_t *keys, const double *values, size_t count, size_
     return padding ? 1 : nonfinite ? 4 : 0;
 }
 
+/* The installed branch backend, if any (tpgp_oracle.h). */
+static orc_branch_fn g_branch_fn;
+static void *g_branch_user;
+
+void orc_set_branch_backend(orc_branch_fn fn, void *user) {
+    g_branch_fn = fn;
+    g_branch_user = user;
+}
+
 static int size_mul(size_t a, size_t b, size_t *out) {
     if (b && a > SIZE_MAX / b)
         return 0;
@@ -226,27 +215,36 @@ int orc_rotate(orc_map *map, size_t i, size_t j, unsigned qi, unsigned qj, doubl
         status = ORC_ENOMEM;
         goto out;
     }
-    /* branch (the only parallel part, as in the reference) */
+    /* branch: from an installed backend (tpgp_rev.c:622-640; its status
+     * already mapped to the engine's), else the loop below, the only parallel
+     * part, as in the reference */
+    if (g_branch_fn) {
+        status = g_branch_fn(g_branch_user, map->keys, map->values, n, words, map->n_spins, i, j,
+                             qi, qj, c, s, raw_keys, raw_values);
+        if (status)
+            goto out;
+    } else {
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1)
 #endif
-    for (size_t k = 0; k < n; k++) {
-        const uint64_t *key = map->keys + k * words;
-        uint64_t *first = raw_keys + 2 * k * words, *second = first + words;
-        memcpy(first, key, words * sizeof(uint64_t));
-        memcpy(second, key, words * sizeof(uint64_t));
-        double v = map->values[k];
-        unsigned pi = site_symbol(key, i), pj = site_symbol(key, j);
-        if (!(anticommutes(qi, pi) ^ anticommutes(qj, pj))) {
-            raw_values[2 * k] = v;
-            raw_values[2 * k + 1] = 0;
-            continue;
+        for (size_t k = 0; k < n; k++) {
+            const uint64_t *key = map->keys + k * words;
+            uint64_t *first = raw_keys + 2 * k * words, *second = first + words;
+            memcpy(first, key, words * sizeof(uint64_t));
+            memcpy(second, key, words * sizeof(uint64_t));
+            double v = map->values[k];
+            unsigned pi = site_symbol(key, i), pj = site_symbol(key, j);
+            if (!(anticommutes(qi, pi) ^ anticommutes(qj, pj))) {
+                raw_values[2 * k] = v;
+                raw_values[2 * k + 1] = 0;
+                continue;
+            }
+            unsigned phase = (phase_of(qi, pi) + phase_of(qj, pj)) & 3u;
+            second[i / 32] ^= (uint64_t)qi << (2 * (i % 32));
+            second[j / 32] ^= (uint64_t)qj << (2 * (j % 32));
+            raw_values[2 * k] = v * c;
+            raw_values[2 * k + 1] = (phase == 1 ? 1.0 : -1.0) * (v * s);
         }
-        unsigned phase = (phase_of(qi, pi) + phase_of(qj, pj)) & 3u;
-        second[i / 32] ^= (uint64_t)qi << (2 * (i % 32));
-        second[j / 32] ^= (uint64_t)qj << (2 * (j % 32));
-        raw_values[2 * k] = v * c;
-        raw_values[2 * k + 1] = (phase == 1 ? 1.0 : -1.0) * (v * s);
     }
     /* finite check (tpgp_rev.c:682-688) */
     for (size_t k = 0; k < slots; k++) {
