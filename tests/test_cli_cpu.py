@@ -1,0 +1,61 @@
+"""The CLI front end without a device (ddevol_gb300/cli/tpgp_gb_cli.c).
+
+Options are checked before the device is touched, as the reference CLI
+checks them before it creates its CUDA context (engine/src/cli_rev.c:437-448, then :476-485): usage, unknown
+options, an END that is not a whole number of steps, a missing edges file and
+an unreadable restart record are reported with exit status 2 on any machine.
+Valid options, or a valid restart record (tests/golden/cli_ring16.tpgpck, the
+reference CLI's own checkpoint), reach the device and then stop with the
+library's message: there is no CPU path.
+"""
+import os
+import subprocess
+
+import pytest
+
+from ddevol_gb300 import build as gbuild
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CHECKPOINT = os.path.join(ROOT, "tests", "golden", "cli_ring16.tpgpck")
+
+
+@pytest.fixture(scope="module")
+def cli():
+    gbuild.build()
+    return gbuild.CLI
+
+
+def run(cli, *args):
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    return subprocess.run([cli, *args], capture_output=True, text=True, env=env, timeout=60)
+
+
+def test_usage_and_option_errors(cli):
+    done = run(cli, "--help")
+    assert done.returncode == 0 and "Usage: tpgp_gb_cli" in done.stderr
+    done = run(cli, "--bogus", "1")
+    assert done.returncode == 2 and "Unknown option: --bogus" in done.stderr
+    done = run(cli, "--dt")  # an option without its value
+    assert done.returncode == 2 and "Usage" in done.stderr
+
+
+def test_argument_checks_come_before_the_device(cli):
+    done = run(cli, "--dt", "0.03", "--time", "0.1")
+    assert done.returncode == 2 and "integer multiple of STEP" in done.stderr
+    done = run(cli, "--model", "edges", "--edges", os.path.join(ROOT, "no-such-file"), "--n", "4")
+    assert done.returncode == 2 and "Usage" in done.stderr
+    done = run(cli, "--threshold", "-1")
+    assert done.returncode == 2 and "Usage" in done.stderr
+    done = run(cli, "--initial", "sideways")
+    assert done.returncode == 2 and "Usage" in done.stderr
+    done = run(cli, "--restart", os.path.join(ROOT, "no-such-checkpoint"))
+    assert done.returncode == 2 and "Restart rejected" in done.stderr
+
+
+def test_valid_runs_need_the_device(cli):
+    done = run(cli, "--model", "j1j2", "--n", "8", "--time", "0.02")
+    assert done.returncode == 2 and "No GB300 device" in done.stderr
+    assert done.stdout == ""  # no CSV header before the device exists
+    # the reference CLI's checkpoint is read on the host, then the device is needed
+    done = run(cli, "--restart", CHECKPOINT)
+    assert done.returncode == 2 and "No GB300 device" in done.stderr
