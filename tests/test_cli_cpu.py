@@ -1,9 +1,10 @@
 """The CLI front end without a device (ddevol_gb300/cli/tpgp_gb_cli.c).
 
 Options are checked before the device is touched, as the reference CLI
-checks them before it creates its CUDA context (engine/src/cli_rev.c:437-448, then :476-485): usage, unknown
-options, an END that is not a whole number of steps, a missing edges file and
-an unreadable restart record are reported with exit status 2 on any machine.
+checks them before it creates its CUDA context (engine/src/cli_rev.c:437-448,
+then :476-485): usage, unknown options, an END that is not a whole number of
+steps, a missing edges file and an unreadable restart record are reported
+with exit status 2 on any machine.
 Valid options, or a valid restart record (tests/golden/cli_ring16.tpgpck, the
 reference CLI's own checkpoint), reach the device and then stop with the
 library's message: there is no CPU path.
