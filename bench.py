@@ -778,6 +778,8 @@ def powder_run(args, eng, seed, budget_s):
     batch.step(args.warmup)
     clusters = batch.autotune()
     tables = bool(batch.lib.tpgp_gb_batch_uses_tables(batch.ptr))
+    widths = sorted({(n + 31) // 32 for n, _ in items})
+    tuning = {w: t for w, t in batch.tuning().items() if w in widths}
     done = args.warmup
     ms, terms_done, launches, steps_timed = 0.0, 0, 0, 0
     t0 = time.perf_counter()
@@ -795,7 +797,7 @@ def powder_run(args, eng, seed, budget_s):
     batch.close()
     return dict(items=len(items), ms=ms, terms=terms_done, launches=launches, steps=steps_timed,
                 reached=done, wall_all=wall_all, sizes=sizes, failed=failed, clusters=clusters,
-                tables=tables)
+                tables=tables, tuning=tuning)
 
 
 def powder_summary(r, peak):
@@ -814,6 +816,7 @@ def powder_summary(r, peak):
                                     "max": int(max(r["sizes"]))},
            "failed_items": r["failed"], "cluster_ctas_per_item": r["clusters"],
            "cta_local_tables": r["tables"], "gpu_launches": r["launches"],
+           "autotuned": {str(w): v for w, v in r.get("tuning", {}).items()},
            "roofline": {"bound": "hbm", "peak": peak, "unit": "GB/s",
                         "achieved": b / (r["ms"] / 1e3) / 1e9,
                         "frac": b / (r["ms"] / 1e3) / 1e9 / peak,

@@ -395,6 +395,18 @@ class Batch:
             raise RuntimeError(f"autotune failed: {err.value.decode()}")
         return {w: self.lib.tpgp_gb_batch_cluster(self.ptr, w) for w in (1, 2, 3, 4)}
 
+    def tuning(self):
+        """Per key width: base cluster size, terms per CTA of the size rule and
+        CTA-local table slots per expected claim (tpgp_gb_batch_get_tuning)."""
+        out = {}
+        for w in (1, 2, 3, 4):
+            c, p, f = C.c_int(), C.c_size_t(), C.c_double()
+            st = self.lib.tpgp_gb_batch_get_tuning(self.ptr, w, C.byref(c), C.byref(p), C.byref(f))
+            if st:
+                raise ValueError(f"batch tuning query failed ({STATUS_NAMES[st]})")
+            out[w] = {"cluster": c.value, "terms_per_cta": p.value, "table_slots_per_claim": f.value}
+        return out
+
     def set_cluster(self, n_words, base, terms_per_cta=0):
         """Base cluster size and terms per CTA of the size rule for one key width."""
         err = C.create_string_buffer(256)

@@ -205,6 +205,9 @@ def _bind(lib):
     lib.tpgp_gb_batch_set_cluster.argtypes = [C.c_void_p, sz, C.c_int, sz, charp, sz]
     lib.tpgp_gb_batch_uses_tables.restype = C.c_int
     lib.tpgp_gb_batch_uses_tables.argtypes = [C.c_void_p]
+    lib.tpgp_gb_batch_get_tuning.restype = C.c_int
+    lib.tpgp_gb_batch_get_tuning.argtypes = [C.c_void_p, sz, C.POINTER(C.c_int),
+                                             C.POINTER(C.c_size_t), C.POINTER(C.c_double)]
     lib.tpgp_gb_batch_max_cluster.restype = C.c_int
     lib.tpgp_gb_batch_max_cluster.argtypes = [C.c_void_p, sz]
     lib.tpgp_gb_batch_item_status.restype = C.c_int

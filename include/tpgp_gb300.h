@@ -345,14 +345,21 @@ tpgp_gb_status tpgp_gb_batch_set_terms(tpgp_gb_batch *batch, size_t item,
  * Returns a non-OK status only for a device failure. */
 tpgp_gb_status tpgp_gb_batch_step(tpgp_gb_batch *batch, size_t steps, double *fid_sums,
                                   char *error, size_t error_capacity);
-/* Picks, per key width, the base cluster size G in {1, 2, 4, 8} with the
- * fastest trial step on the current maps, then whether bound-ledger items
- * that fit run in CTA-local hash tables or on the clusters (trial steps are
- * not committed).  tpgp_gb_batch_cluster returns the base size,
- * tpgp_gb_batch_uses_tables 1 when the tables are in use. */
+/* Picks, per key width, from the fastest trial step on the current maps
+ * (trial steps are not committed): the base cluster size G in {1, 2, 4, 8};
+ * the terms per CTA of the cluster-size rule in {4096, 8192, 16384} (16, 32
+ * or 64 terms per thread); whether bound-ledger items that fit run in
+ * CTA-local hash tables or on the clusters; and the tables' size, 2 or 4
+ * slots per expected claimed key (the table is also the tile of the item's
+ * closing block sort).  Results are the same under every choice.
+ * tpgp_gb_batch_cluster returns the base size, tpgp_gb_batch_uses_tables 1
+ * when the tables are in use, tpgp_gb_batch_get_tuning all of a width's
+ * choices (NULL outputs are skipped). */
 tpgp_gb_status tpgp_gb_batch_autotune(tpgp_gb_batch *batch, char *error, size_t error_capacity);
 int tpgp_gb_batch_cluster(const tpgp_gb_batch *batch, size_t n_words);
 int tpgp_gb_batch_uses_tables(const tpgp_gb_batch *batch);
+tpgp_gb_status tpgp_gb_batch_get_tuning(const tpgp_gb_batch *batch, size_t n_words, int *cluster,
+                                        size_t *terms_per_cta, double *table_slots_per_claim);
 /* Sets the base cluster size (a power of two up to max_cluster) and the
  * terms per CTA of the size rule (0: 8192) for one key width. */
 tpgp_gb_status tpgp_gb_batch_set_cluster(tpgp_gb_batch *batch, size_t n_words, int base,

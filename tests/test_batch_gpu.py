@@ -90,6 +90,10 @@ def test_batch_cluster_sizes_agree(engine, shape, smem_off):
     if shape == "autotune":
         chosen = batch.autotune()
         assert chosen[1] in (1, 2, 4, 8)
+        tuned = batch.tuning()[1]
+        assert tuned["cluster"] == chosen[1]
+        assert tuned["terms_per_cta"] in (4096, 8192, 16384)
+        assert tuned["table_slots_per_claim"] in (2.0, 4.0)
     fids = batch.step(3)
     assert batch.max_cluster(1) in (8, 16)
     for k, (n, terms, thr) in enumerate(items):
