@@ -53,6 +53,48 @@ def test_argument_checks_come_before_the_device(cli):
     assert done.returncode == 2 and "Restart rejected" in done.stderr
 
 
+REST = ["--model", "edges", "--n", "16", "--initial", "local", "--dt", "0.01",
+        "--threshold", "1e-6"]
+
+
+def capped_record(tmp_path, cap):
+    """The reference CLI's record with a term cap set (written by the library, host only)."""
+    import ctypes as C
+
+    from ddevol_gb300 import native
+    lib = native.load()
+    rec = native.GbCheckpoint()
+    err = C.create_string_buffer(256)
+    assert lib.tpgp_gb_checkpoint_load(CHECKPOINT.encode(), C.byref(rec), err, 256) == 0
+    rec.max_terms = cap
+    out = str(tmp_path / "capped.tpgpck")
+    assert lib.tpgp_gb_checkpoint_write(out.encode(), C.byref(rec), err, 256) == 0, err.value
+    lib.tpgp_gb_checkpoint_free(C.byref(rec))
+    return out
+
+
+def test_restart_options_must_match_the_record(cli, tmp_path):
+    """cli_rev.c:365-399: options given again on a restart must equal the
+    record's, except that the horizon may grow and the cap may be raised."""
+    def restart(*extra, record=CHECKPOINT):
+        return run(cli, "--restart", record, *extra)
+
+    # the record: edges model, 16 spins, local X_0, dt 0.01, threshold 1e-6,
+    # 20 steps, no cap
+    same = restart(*REST, "--time", "0.3")
+    assert same.returncode == 2 and "No GB300 device" in same.stderr
+    for bad in (["--dt", "0.02"], ["--threshold", "1e-5"], ["--initial", "global"],
+                ["--n", "17"], ["--model", "ring"], ["--time", "0.1"], ["--cap", "1000"],
+                ["--drop-budget", "1"], ["--j2", "0.5"]):
+        done = restart(*bad)
+        assert done.returncode == 2 and "Restart rejected" in done.stderr, bad
+    capped = capped_record(tmp_path, 5000)
+    assert "No GB300 device" in restart("--cap", "9000", record=capped).stderr  # raised
+    assert "No GB300 device" in restart("--cap", "5000", record=capped).stderr
+    assert "Restart rejected" in restart("--cap", "4000", record=capped).stderr  # lowered
+    assert "No GB300 device" in restart("--cap", "0", record=capped).stderr  # 0 lifts the cap
+
+
 def test_valid_runs_need_the_device(cli):
     done = run(cli, "--model", "j1j2", "--n", "8", "--time", "0.02")
     assert done.returncode == 2 and "No GB300 device" in done.stderr
