@@ -80,11 +80,11 @@ def test_restart_options_must_match_the_record(cli, tmp_path):
         return run(cli, "--restart", record, *extra)
 
     # the record: edges model, 16 spins, local X_0, dt 0.01, threshold 1e-6,
-    # 20 steps, no cap
+    # 20 steps, the reference CLI's default cap of 10^6 terms
     same = restart(*REST, "--time", "0.3")
     assert same.returncode == 2 and "No GB300 device" in same.stderr
     for bad in (["--dt", "0.02"], ["--threshold", "1e-5"], ["--initial", "global"],
-                ["--n", "17"], ["--model", "ring"], ["--time", "0.1"], ["--cap", "1000"],
+                ["--n", "17"], ["--model", "ring"], ["--time", "0.1"], ["--cap", "1000"],  # a lower cap
                 ["--drop-budget", "1"], ["--j2", "0.5"]):
         done = restart(*bad)
         assert done.returncode == 2 and "Restart rejected" in done.stderr, bad
