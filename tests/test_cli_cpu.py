@@ -95,6 +95,36 @@ def test_restart_options_must_match_the_record(cli, tmp_path):
     assert "No GB300 device" in restart("--cap", "0", record=capped).stderr  # 0 lifts the cap
 
 
+MODELS = {
+    "ring_n6": [],
+    "ring_n9": ["--model", "ring", "--n", "9"],
+    "j1j2_n8": ["--model", "j1j2", "--n", "8"],
+    "j1j2_n10_j2_0125": ["--model", "j1j2", "--n", "10", "--j2", "0.125"],
+    "ising_n5": ["--model", "ising", "--n", "5"],
+    "xy_n7": ["--model", "xy", "--n", "7"],
+    "cubic_l3": ["--model", "cubic", "--linear-size", "3"],
+    "cubic_l4": ["--model", "cubic", "--linear-size", "4"],
+    "edges_ring16": ["--model", "edges", "--edges",
+                     os.path.join(ROOT, "tests", "golden", "ring16.edges"), "--n", "16"],
+}
+
+
+@pytest.mark.parametrize("name", sorted(MODELS))
+def test_models_build_the_reference_term_lists(cli, name):
+    """Every model's term list (order, sites, labels, h bit for bit) as the
+    reference CLI builds it (cli_rev.c:108-245), from the records of its own
+    one-step runs (tests/golden/cli_terms.npz, made by make_cli.py)."""
+    import numpy as np
+    golden = np.load(os.path.join(ROOT, "tests", "golden", "cli_terms.npz"))
+    done = run(cli, *MODELS[name], "--list-terms")
+    assert done.returncode == 0, done.stderr
+    rows = [line.split() for line in done.stdout.splitlines()]
+    ijq = np.array([[int(x) for x in r[:4]] for r in rows], np.uint64).reshape(-1, 4)
+    h = np.array([float.fromhex(r[4]) for r in rows], np.float64)
+    assert np.array_equal(ijq, golden[name + "_ijq"])
+    assert np.array_equal(h.view(np.uint64), golden[name + "_h"].view(np.uint64))
+
+
 def test_valid_runs_need_the_device(cli):
     done = run(cli, "--model", "j1j2", "--n", "8", "--time", "0.02")
     assert done.returncode == 2 and "No GB300 device" in done.stderr
