@@ -40,6 +40,29 @@ def test_usage_and_option_errors(cli):
     assert done.returncode == 2 and "Usage" in done.stderr
 
 
+def test_reference_cli_options(cli, tmp_path):
+    """The reference CLI's other options: --backend cuda (its GPU backend's
+    name) selects this device path and a CPU backend is refused; --threads is
+    accepted; the MPFR-only modes are refused as a reference build without
+    MPFR refuses them; a walltime stop needs a checkpoint path distinct from
+    the CSV (cli_rev.c:426-431, 450-462)."""
+    assert "No GB300 device" in run(cli, "--backend", "cuda", "--threads", "4").stderr
+    for args, message in ((["--backend", "serial"], "device path only"),
+                          (["--validated"], "requires MPFR"),
+                          (["--residual-depth", "2"], "require MPFR"),
+                          (["--max-fid-bound", "0.1"], "MPFR-enclosed"),
+                          (["--walltime", "5"], "require a checkpoint path"),
+                          (["--checkpoint", str(tmp_path / "a"), "--output", str(tmp_path / "a")],
+                           "distinct from CSV"),
+                          (["--checkpoint-every", "0"], "Usage"),
+                          (["--walltime", "-1"], "Usage")):
+        done = run(cli, *args)
+        assert done.returncode == 2 and message in done.stderr, (args, done.stderr)
+    ok = run(cli, "--walltime", "5", "--checkpoint", str(tmp_path / "w.tpgpck"),
+             "--checkpoint-seconds", "1")
+    assert ok.returncode == 2 and "No GB300 device" in ok.stderr
+
+
 def test_argument_checks_come_before_the_device(cli):
     done = run(cli, "--dt", "0.03", "--time", "0.1")
     assert done.returncode == 2 and "integer multiple of STEP" in done.stderr
