@@ -1018,6 +1018,17 @@ def run_reference(args, dist):
               f"one Strang step from a different offset ({tot_rot} rotations, {tot_terms} input "
               f"terms, {tot_s:.1f} s of rotation calls), each rotation applied to the "
               f"{len(v)}-term window state")
+    # the serial backend beside the threaded one (the reference's serial and
+    # openmp backends differ only in the branch loop's threads)
+    s_terms, s_secs, s_rots, s_stride = cpu_sample(impl, k, v, cfg["n"], terms, cfg["dt"],
+                                                   cfg["threshold"], min(5.0, budget), 1,
+                                                   offset=3)
+    backends = {
+        "threads": {"value": value, "threads": cores,
+                    "how": "branch loop on all host threads (OpenMP), sort and merge serial"},
+        "serial": {"value": s_terms / s_secs, "threads": 1,
+                   "sample": f"every {s_stride}th rotation of the step ({s_rots} rotations)"},
+    }
     return {
         "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps,
@@ -1027,6 +1038,7 @@ def run_reference(args, dist):
         "window": {"ledger": "exact (sequential)", "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
                          "sample": sample},
+        "backends": backends,
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "libraries": repo_libraries(),
     }
