@@ -51,6 +51,9 @@ def test_reference_arm_runs_on_the_window_state_without_the_gpu_library():
     assert line["config"]["window_state_terms"] == 100947
     assert line["config"]["rotations_per_step"] == 2 * len(cfg["terms"]())
     assert "every" in line["cpu_baseline"]["sample"] and line["value"] > 0
+    # the serial backend beside the threaded one
+    assert line["backends"]["serial"]["threads"] == 1 and line["backends"]["serial"]["value"] > 0
+    assert line["backends"]["threads"]["value"] == line["value"]
 
 
 def test_strided_sample_spreads_over_the_step():
