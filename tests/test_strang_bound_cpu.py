@@ -33,3 +33,21 @@ def test_library_strang_bound_matches_reference():
             assert np.float64(got).view(np.uint64) == np.float64(want).view(np.uint64), name
         checked += 1
     assert checked >= 20
+
+
+def test_oracle_strang_bound_matches_reference(oracle):
+    """The oracle's restatement (orc_strang_bound, orc_strang_bound_taylor),
+    which the GPU enclosure test uses, bitwise the reference's on the same lists."""
+    z = dict(np.load(GOLDEN))
+    for name in z["strang_names"]:
+        p = "strang_" + str(name) + "_"
+        terms = [(int(a), int(b), int(c), int(d), float(h))
+                 for (a, b, c, d), h in zip(z[p + "terms"].reshape(-1, 4), z[p + "h"])]
+        for taylor, key in ((False, "bound"), (True, "taylor")):
+            got = oracle.strang_bound(terms, float(z[p + "dt"]), taylor_only=taylor)
+            want = float(z[p + key])
+            if math.isnan(want):
+                assert math.isnan(got), (name, key)
+            else:
+                assert np.float64(got).view(np.uint64) == np.float64(want).view(np.uint64), \
+                    (name, key)
