@@ -62,3 +62,25 @@ def test_serving_request_matches_all_pairs_builders():
         assert n == n2 and terms == build(n, scale=scale, cutoff=3)
         assert 1e-6 <= thr <= 1e-4 and 20 <= steps <= 80 and dt == 0.01
     assert seen == {True, False}
+
+
+def test_term_builders_match_the_reference_cli():
+    """The benchmark's 16-spin term list is bitwise the reference CLI's for the
+    committed edges file, and the J1-J2 builder reproduces the CLI's j1j2
+    model (its d = 2 J convention: J = 1/2, J2 = ratio / 2), from the
+    reference CLI's own records (tests/golden/cli_terms.npz)."""
+    import os
+
+    import numpy as np
+    golden = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                  "cli_terms.npz"))
+
+    def same(terms, name):
+        ijq = np.array([t[:4] for t in terms], np.uint64)
+        h = np.array([t[4] for t in terms], np.float64)
+        return (np.array_equal(ijq, golden[name + "_ijq"]) and
+                np.array_equal(h.view(np.uint64), golden[name + "_h"].view(np.uint64)))
+
+    assert same(H.ring_j1j2(16), "edges_ring16")
+    assert same(H.ring_j1j2(10, 0.5, 0.0625), "j1j2_n10_j2_0125")
+    assert same(H.ring_j1j2(8, 0.5, 0.15), "j1j2_n8")
