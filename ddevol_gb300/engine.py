@@ -39,11 +39,11 @@ def _f64p(a):
 def options(threshold=0.0, max_terms=0, max_drop_l2=0.0, exact_ledger=True, use_graphs=True,
             wait_polls=0):
     """tpgp_gb_options.  exact_ledger=True: the reference's sequential
-    removed-weight ledger, bitwise (sorted per-rotation kernels);
-    exact_ledger=False: the fixed-point bound ledger, which also selects the
-    hash-table step for maps up to 6e5 terms.  Keys, values and FIDs are the
-    same either way.  wait_polls: poll limit of the device-side waits (0:
-    the defaults)."""
+    removed-weight ledger, bitwise; exact_ledger=False: the fixed-point bound
+    ledger (a certified upper bound a few ulps from it).  Keys, values and
+    FIDs are the same either way, and with either ledger maps up to 6e5 terms
+    step on the hash-table kernels.  wait_polls: poll limit of the
+    device-side waits (0: the defaults)."""
     return GbOptions(float(threshold), int(max_terms), float(max_drop_l2), int(bool(exact_ledger)),
                      int(bool(use_graphs)), int(wait_polls))
 

@@ -54,15 +54,18 @@ typedef struct {
  * in tpgp_options (engine/include/tpgp_rev.h:36-45).
  *   exact_ledger = 1: the removed-weight sums are accumulated in the
  *     reference's sequential key order, so the ledger is bitwise equal to the
- *     CPU engine's; one GPU thread walks the removed terms of each rotation.
+ *     CPU engine's: each rotation's removed terms are logged, sorted by key
+ *     and summed after the step's rotations with warp-parallel upward sums
+ *     that give the sequential chain's bits.
  *   exact_ledger = 0: each removed |v| and v^2 is rounded up to a multiple
  *     of a fixed-point unit set by the threshold and summed exactly in 128-bit
  *     integers, then converted up once per rotation: deterministic,
  *     independent of the launch shape, a rigorous upper bound on the removed
  *     weight a few ulps from the sequential sum.  Keys, values, FIDs and the
- *     integer ledger fields are the same in both modes.  With this mode,
- *     steps of maps up to 6e5 terms run the hash-table step (one kernel per
- *     rotation, no sort; TPGP_GB_HASH=0 disables it).
+ *     integer ledger fields are the same in both modes.
+ *   With either ledger, steps of maps up to 6e5 terms run the hash-table step
+ *   (one kernel per rotation, no sort; TPGP_GB_HASH=0 disables it) and larger
+ *   maps the sorted per-rotation kernels.
  *   use_graphs = 1: each Strang step's kernel sequence is captured once as a
  *     CUDA graph and replayed.
  *   wait_polls: how many times a device-side wait (decoupled look-back,
