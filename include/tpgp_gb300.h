@@ -84,9 +84,9 @@ typedef struct {
 typedef struct tpgp_gb_context tpgp_gb_context;
 typedef struct tpgp_gb_map tpgp_gb_map;
 
-/* Library and device.  compiled() returns 1 (the library has its device code).  create() binds one
- * device (index as CUDA_VISIBLE_DEVICES numbers it) and a stream; NULL with
- * a message when the device is missing.  Replaces the context part of
+/* Library and device.  compiled() returns 1 (the library has its device
+ * code).  create() binds one device (index as CUDA_VISIBLE_DEVICES numbers
+ * it) and a stream; NULL with a message when the device is missing.  Replaces the context part of
  * engine/include/tpgp_cuda_rev.h:20-23 for the device-resident path. */
 int tpgp_gb_compiled(void);
 tpgp_gb_options tpgp_gb_default_options(void);
@@ -187,10 +187,11 @@ typedef struct {
  * reference's upper_l2 without MPFR, :57-62).  A nonfinite child or merged
  * radius is ENUMERIC; arithmetic_enclosed becomes 0 (no MPFR enclosure).
  * The ledger is the exact one whatever options.exact_ledger says.  Runs on
- * the hash-table step at any map size.  Rotations up to the first invalid
- * one (site, generator, or a nonfinite or negative factor or radius) are
- * applied and the call then returns EINVAL with the map and ledger
- * unchanged; an empty map is a no-op. */
+ * the hash-table step at any map size.  A list with an invalid rotation
+ * (site, generator, or a nonfinite or negative factor or radius) returns
+ * EINVAL after the rotations before it are computed, with the map and
+ * ledger unchanged (their statuses come first, as in the reference's
+ * order); an empty map is a no-op. */
 tpgp_gb_status tpgp_gb_rotate_enclosed(tpgp_gb_map *map, const tpgp_gb_rotation *rotations,
                                        size_t count, const tpgp_gb_options *options,
                                        tpgp_gb_ledger *ledger, char *error, size_t error_capacity);
@@ -245,7 +246,8 @@ tpgp_gb_status tpgp_gb_checkpoint_load(const char *path, tpgp_gb_checkpoint *rec
 void tpgp_gb_checkpoint_free(tpgp_gb_checkpoint *record);
 /* Downloads a device map and writes it with its run state as the reference
  * CLI's save_current does (engine/src/cli_rev.c:72-106): backend 4 (CUDA),
- * one thread, no validated mode, no residual bound. */
+ * one thread, no validated mode, no residual bound, linear size the cubic
+ * model's lattice edge (else 3, the reference CLI's default). */
 tpgp_gb_status tpgp_gb_checkpoint_save(const char *path, const tpgp_gb_map *map,
                                        const tpgp_gb_term *terms, size_t count, const char *model,
                                        double j2, double dt, const tpgp_gb_options *options,
