@@ -326,8 +326,11 @@ void tpgp_gb_kernel_profile(const tpgp_gb_map *map, double *milliseconds, size_t
  * that runs the item's whole rotation list, and the step's transfers and
  * launches are replayed from a CUDA graph.  G grows with the item's map (one
  * CTA per 8192 terms by default, a power of two from the width's base size up
- * to 16 where the device runs 16-CTA clusters, else 8).  Results per item are those of
- * tpgp_gb_strang_step on that item alone (keys, values, FID bitwise).
+ * to 16 where the device runs 16-CTA clusters, else 8).  Bound-ledger items
+ * whose step fits a CTA-local hash table run there instead, one CTA per
+ * item (TPGP_GB_BATCH_SMEM=0 keeps every item on the clusters).  Results per
+ * item are those of tpgp_gb_strang_step on that item alone (keys, values,
+ * FID bitwise).
  * Items fail independently: item_status() is the tpgp_status of an item's
  * failed step (the item then stays at its last accepted step and is
  * skipped), 0 while healthy. */
