@@ -8,11 +8,11 @@ GPU: requests arriving staggered and outnumbering the slots queue, take
 slots of a sufficient width as earlier solves finish, and run interleaved;
 each request's per-step FIDs must be bitwise the oracle's on the request
 alone at its own spin count, however it was scheduled; a memory budget that
-fits one projected solve admits one at a time.
+fits one projected solve admits one at a time; a failing request fails
+alone.
 """
 import ctypes as C
 import os
-import shutil
 import subprocess
 import types
 
@@ -97,3 +97,20 @@ def test_queueing_reuses_slots_and_memory_budget_admits_one(server, oracle):
     assert all(b[0] >= a[1] for a, b in zip(spans, spans[1:]))  # one at a time
     for r in range(len(reqs)):
         assert np.array_equal(fids1[r].view(np.uint64), fids[r].view(np.uint64)), r
+
+
+def test_failing_requests_do_not_disturb_the_others(server, oracle):
+    """A request that hits its term cap fails on its own (ECAP, its slot
+    freed for the next request), one with an unusable time step is refused at
+    admission (ENUMERIC: dt/2 inexact, as tpgp_strang_step refuses it); every
+    other request's FIDs stay bitwise the oracle's."""
+    reqs = make_requests(8, seed=23, gap=0.001)
+    reqs[2]["options"] = options(reqs[2]["options"].threshold, max_terms=3, exact_ledger=False)
+    reqs[5]["dt"] = 5e-324
+    resp, fids, stats = server.serve(reqs, slots=(1, 1, 1))
+    assert resp[2]["status"] == 3 and resp[5]["status"] == 4
+    for r, q in enumerate(reqs):
+        if r in (2, 5):
+            continue
+        assert resp[r]["status"] == 0
+        assert np.array_equal(fids[r].view(np.uint64), oracle_fids(oracle, q).view(np.uint64)), r
