@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from ddevol_gb300 import hamiltonians as H
-from ddevol_gb300.engine import Batch, GbLedger, options
+from ddevol_gb300.engine import Batch, options
 
 pytestmark = pytest.mark.gpu
 

@@ -6,7 +6,6 @@ into oracle/_ref where the checkout was present); a damaged record is
 rejected and leaves the destination untouched."""
 import ctypes as C
 import os
-import shutil
 
 import numpy as np
 import pytest
