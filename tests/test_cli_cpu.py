@@ -63,6 +63,18 @@ def test_reference_cli_options(cli, tmp_path):
     assert ok.returncode == 2 and "No GB300 device" in ok.stderr
 
 
+def test_option_values_are_taken_whole(cli):
+    """As the reference CLI parses them (cli_rev.c:133-149): a real must be a
+    finite decimal with nothing after it, a count an unsigned decimal."""
+    for args in (["--dt", "0.01x"], ["--dt", "nan"], ["--time", "inf"], ["--n", "-3"],
+                 ["--n", "8.5"], ["--cap", ""], ["--threads", "0"], ["--exact-ledger", "2"],
+                 ["--checkpoint-every", "ten"], ["--linear-size", "+4"]):
+        done = run(cli, *args)
+        assert done.returncode == 2 and "Usage" in done.stderr, args
+    assert "No GB300 device" in run(cli, "--dt", "1e-2", "--time", "0.04", "--threads",
+                                    "8", "--exact-ledger", "0").stderr
+
+
 def test_argument_checks_come_before_the_device(cli):
     done = run(cli, "--dt", "0.03", "--time", "0.1")
     assert done.returncode == 2 and "integer multiple of STEP" in done.stderr
