@@ -232,7 +232,8 @@ typedef struct {
     char model[32];
     double j2;
     size_t linear_size, resumed_from_step, prior_total_steps, prior_max_terms;
-    int stop_reason; /* 0 running, 1 complete, 2 walltime, 3 signal, 4 resource, 5 numerical, 6 accuracy */
+    int stop_reason; /* 0 running, 1 complete, 2 walltime, 3 signal, 4 resource,
+                        5 numerical, 6 accuracy */
     tpgp_gb_status last_status;
 } tpgp_gb_checkpoint;
 
