@@ -114,3 +114,7 @@ def test_restart_pause_and_cap_stop(cli, tmp_path):
     assert final_row(raised) == final_row(full)
     # lowering the cap on a restart is refused
     run(cli, "--restart", cc, "--cap", "100", "--output", str(tmp_path / "c3.csv"), code=2)
+    # an existing CSV is never overwritten
+    kept = full.read_text()
+    refused = run(cli, *ARGS, "--time", "0.02", "--output", str(full), code=2)
+    assert "File exists" in refused.stderr and full.read_text() == kept
