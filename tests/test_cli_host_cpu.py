@@ -13,7 +13,8 @@ logic is then checked against the reference CLI's behaviour:
 * a walltime pause checkpoints and exits 75, and resuming completes the run
   as if uninterrupted;
 * a cap stop exits 1 with a record, and a restart with a raised cap
-  continues to the uninterrupted run's final row.
+  continues to the uninterrupted run's final row;
+* an existing CSV is never overwritten.
 """
 import csv
 import io
