@@ -48,12 +48,12 @@ def test_reference_cli_options(cli, tmp_path):
     the CSV (cli_rev.c:426-431, 450-462)."""
     assert "No GB300 device" in run(cli, "--backend", "cuda", "--threads", "4").stderr
     for args, message in ((["--backend", "serial"], "device path only"),
-                          (["--validated"], "requires MPFR"),
-                          (["--residual-depth", "2"], "require MPFR"),
+                          (["--validated"], "needs MPFR"),
+                          (["--residual-depth", "2"], "needs the MPFR"),
                           (["--max-fid-bound", "0.1"], "MPFR-enclosed"),
-                          (["--walltime", "5"], "require a checkpoint path"),
+                          (["--walltime", "5"], "needs --checkpoint"),
                           (["--checkpoint", str(tmp_path / "a"), "--output", str(tmp_path / "a")],
-                           "distinct from CSV"),
+                           "must differ from --output"),
                           (["--checkpoint-every", "0"], "Usage"),
                           (["--walltime", "-1"], "Usage")):
         done = run(cli, *args)
@@ -77,7 +77,7 @@ def test_option_values_are_taken_whole(cli):
 
 def test_argument_checks_come_before_the_device(cli):
     done = run(cli, "--dt", "0.03", "--time", "0.1")
-    assert done.returncode == 2 and "integer multiple of STEP" in done.stderr
+    assert done.returncode == 2 and "whole number of --dt steps" in done.stderr
     done = run(cli, "--model", "edges", "--edges", os.path.join(ROOT, "no-such-file"), "--n", "4")
     assert done.returncode == 2 and "Usage" in done.stderr
     done = run(cli, "--threshold", "-1")
@@ -85,7 +85,7 @@ def test_argument_checks_come_before_the_device(cli):
     done = run(cli, "--initial", "sideways")
     assert done.returncode == 2 and "Usage" in done.stderr
     done = run(cli, "--restart", os.path.join(ROOT, "no-such-checkpoint"))
-    assert done.returncode == 2 and "Restart rejected" in done.stderr
+    assert done.returncode == 2 and "Cannot restart" in done.stderr
 
 
 REST = ["--model", "edges", "--n", "16", "--initial", "local", "--dt", "0.01",
@@ -122,11 +122,11 @@ def test_restart_options_must_match_the_record(cli, tmp_path):
                 ["--n", "17"], ["--model", "ring"], ["--time", "0.1"], ["--cap", "1000"],  # a lower cap
                 ["--drop-budget", "1"], ["--j2", "0.5"]):
         done = restart(*bad)
-        assert done.returncode == 2 and "Restart rejected" in done.stderr, bad
+        assert done.returncode == 2 and "Cannot restart" in done.stderr, bad
     capped = capped_record(tmp_path, 5000)
     assert "No GB300 device" in restart("--cap", "9000", record=capped).stderr  # raised
     assert "No GB300 device" in restart("--cap", "5000", record=capped).stderr
-    assert "Restart rejected" in restart("--cap", "4000", record=capped).stderr  # lowered
+    assert "Cannot restart" in restart("--cap", "4000", record=capped).stderr  # lowered
     assert "No GB300 device" in restart("--cap", "0", record=capped).stderr  # 0 lifts the cap
 
 
